@@ -1,0 +1,357 @@
+"""Benchmark: primary+shadow Mrays/s of the octree ray-cast path on one GB300.
+
+Workload (default): the room scene, 20,000,000 seeded points (closed room +
+200 boxes + 100 spheres), octree depth 12, basecube 1800, rendered from 16
+camera poses on a seeded Catmull-Rom spline at 1920x1080. One step renders the
+16 views in one batch (one kernel launch): primary ray, shadow ray, shading and
+light flare per pixel, exactly as the reference fragment shader
+(src/qubatron/shaders/octree_fsh.c:399-464).
+
+Rays per step = primary rays (one per pixel) + shadow rays actually cast
+(pixels whose primary hit has t > 0) + flare rays, counted from the per-pixel
+flags of one untimed frame.
+
+value: device-resident inputs and outputs, CUDA events around each step on the
+       launching stream, L2 flushed between steps (outside the events).
+e2e:   the same views through the public C ABI with host output buffers
+       (qbc_render_views, outputs_on_device = 0): device work plus the copy of
+       every RGBA8 frame back to pinned host memory, wall clock per step.
+cpu_baseline: the C oracle (a restatement of the shader, OpenMP over all host
+       cores) on a seeded sample of the same pixels.
+
+--impl reference times that CPU implementation alone (the reference's own
+path is GLSL and cannot run without a graphics stack).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "room20m_1920x1080x16"
+L2_BYTES = 129 * 1024 * 1024
+FALLBACK_HBM_GBS = 6800.0
+# algorithmic bytes: a node visit reads one 32-byte child
+# block of one tree; a leaf reads a 4-byte model index and a 12-byte colour
+# and 12-byte normal; every pixel writes 4 bytes of RGBA8
+BYTES_PER_VISIT = 32
+BYTES_PER_LEAF = 28
+BYTES_PER_PIXEL_OUT = 4
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = os.path.join("/tmp", f"qb_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def prepare(workload_name: str):
+    from qubatron_gb300 import scenes
+    w = scenes.WORKLOADS[workload_name]
+    t = time.time()
+    scene = scenes.make_scene(w.scene)
+    views = scenes.workload_views(w)
+    return w, scene, views, time.time() - t
+
+
+def count_rays(flags: np.ndarray) -> int:
+    f = flags.astype(np.uint32)
+    primary = f.size
+    shadow = int(((f >> 2) & 1).sum())
+    flare = int(((f >> 5) & 1).sum())
+    return primary + shadow + flare
+
+
+def cpu_sample(scene, views, budget_s: float, seed: int = 7):
+    """The oracle on a seeded pixel sample of the views, all host cores."""
+    from oracle import qbo
+    threads = os.cpu_count() or 1
+    sc = qbo.Scene(scene.nodes, scene.colors, scene.normals)
+    ov = [qbo.QboView.from_bytes(v.to_bytes()) for v in views]
+    rng = np.random.default_rng(seed)
+
+    def run(per_view: int):
+        rays, t0 = 0, time.perf_counter()
+        for v in ov:
+            px = rng.integers(0, v.width_px, per_view).astype(np.int32)
+            py = rng.integers(0, v.height_px, per_view).astype(np.int32)
+            out = qbo.render_pixels(sc, v, px, py, threads)
+            rays += count_rays(out["flags"])
+        return rays, time.perf_counter() - t0
+
+    rays, dt = run(256)  # calibration
+    rate = rays / max(dt, 1e-6)
+    per_view = int(max(256, min(200000, budget_s * rate / (len(ov) * 2.05))))
+    rays, dt = run(per_view)
+    return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": f"{per_view} seeded pixels x {len(ov)} views of the same workload ({rays} rays, {dt:.1f} s)",
+            "seconds": dt, "rays": rays}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    w, scene, views, _ = prepare(WORKLOAD)
+    # each step: a bounded sample (~8 s) of the workload's pixels
+    from oracle import qbo  # noqa: F401
+    times, rays_total = [], 0
+    res = None
+    for step in range(args.warmup + args.steps):
+        res = cpu_sample(scene, views, budget_s=8.0, seed=100 + step)
+        if step >= args.warmup:
+            times.append(res["seconds"])
+            rays_total += res["rays"]
+    value = rays_total / sum(times) / 1e6
+    line = {
+        "impl": "reference", "metric": "primary+shadow Mrays/s", "value": value, "unit": "Mrays/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * statistics.mean(times) if times else None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "config": {"workload": WORKLOAD, "points": scene.points.shape[0], "nodes": int(scene.nodes.shape[0]),
+                   "resolution": f"{w.width}x{w.height}", "views": len(views), "depth": 12, "basecube": 1800.0},
+        "cpu_baseline": {k: res[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's own path is a GLSL fragment shader (no graphics stack here); this is its C "
+                "restatement (oracle/) on all host cores, per step a seeded pixel sample of the workload",
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    import torch
+    import qubatron_gb300 as qb
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    w, scene, views, prep_s = prepare(WORKLOAD)
+
+    ctx = qb.OctreeGLC(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    ctx.upload_model(False, scene.colors, scene.normals)
+    ctx.upload_octree(False, scene.nodes)
+
+    # device outputs
+    frames = [torch.empty((v.height_px, v.width_px, 4), dtype=torch.uint8, device="cuda") for v in views]
+    outs = []
+    for f in frames:
+        o = qb.Outputs()
+        o.rgba8 = f.data_ptr()
+        outs.append(o)
+
+    # one untimed instrumented pass: rays cast and node visits per step
+    flags = [torch.empty((v.height_px, v.width_px), dtype=torch.int32, device="cuda") for v in views]
+    visits = [torch.empty((v.height_px, v.width_px, 4), dtype=torch.int32, device="cuda") for v in views]
+    isp = [torch.empty((v.height_px, v.width_px, 4), dtype=torch.float32, device="cuda") for v in views]
+    inst = []
+    for f, fl, vi, ip in zip(frames, flags, visits, isp):
+        o = qb.Outputs()
+        o.rgba8 = f.data_ptr()
+        o.flags = fl.data_ptr()
+        o.visits = vi.data_ptr()
+        o.leaf = 0
+        o.isp = ip.data_ptr()
+        inst.append(o)
+    ctx.render_views(views, inst, on_device=True)
+    torch.cuda.synchronize()
+    rays = 0
+    vis_total = 0
+    leaves = 0
+    for fl, vi in zip(flags, visits):
+        f = fl.cpu().numpy().view(np.uint32)
+        rays += count_rays(f)
+        leaves += int((f & 1).sum()) + int(((f >> 3) & 1).sum())
+        vis_total += int(vi.to(torch.int64).sum().item())
+    pixels = sum(v.width_px * v.height_px for v in views)
+    alg_bytes = vis_total * BYTES_PER_VISIT + leaves * BYTES_PER_LEAF + pixels * BYTES_PER_PIXEL_OUT
+    del flags, visits, isp
+
+    flush = torch.empty(2 * L2_BYTES, dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        ctx.render_views(views, outs, on_device=True)
+    torch.cuda.synchronize()
+
+    l0 = ctx.launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            ctx.render_views(views, outs, on_device=True)
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    launches = ctx.launch_count() - l0
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    ms = statistics.mean(step_ms)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * rays / (ms / 1000.0) / 1e6
+
+    # e2e through the public API with pinned host outputs
+    host = [torch.empty((v.height_px, v.width_px, 4), dtype=torch.uint8, pin_memory=True) for v in views]
+    houts = []
+    for h in host:
+        o = qb.Outputs()
+        o.rgba8 = h.data_ptr()
+        houts.append(o)
+    for _ in range(2):
+        ctx.render_views(views, houts, on_device=False)
+    e2e_t = []
+    for k in range(max(3, args.steps)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.render_views(views, houts, on_device=False)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = statistics.mean(e2e_t)
+    d2h = sum(h.numel() for h in host)
+    h2d = len(views) * 132  # qbc_view uniforms, passed as launch parameters
+
+    hbm, peak_kind = peaks()
+    achieved = alg_bytes / (ms / 1000.0) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "render_kernel_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            t = json.load(f)
+        if t.get("workload") == WORKLOAD:
+            traffic = t.get("dram_bytes_per_launch")
+
+    line = {
+        "metric": "primary+shadow Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
+        "config": {"workload": WORKLOAD, "points": int(scene.points.shape[0]), "nodes": int(scene.nodes.shape[0]),
+                   "resolution": f"{w.width}x{w.height}", "views": len(views), "depth": 12, "basecube": 1800.0,
+                   "rays_per_step": rays, "nominal_2wh_rays_per_step": 2 * pixels,
+                   "l2": "flushed between steps (2x L2 write, outside the timed events); node arrays "
+                         f"{scene.nodes.shape[0] * 36 / 1e9:.2f} GB > L2",
+                   "parallelism": "replicas only" if world > 1 else "single GPU",
+                   "prep_seconds": round(prep_s, 1)},
+        "e2e": {"value": world * rays / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic, "peak_kind": f"{peak_kind} (burst copy)",
+                     "algorithmic_bytes_per_launch": alg_bytes},
+        "clocks": clk.summary(),
+        "step_ms": [round(x, 4) for x in step_ms],
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = {k: v for k, v in cpu_sample(scene, views, budget_s=args.cpu_seconds).items()
+                                if k not in ("seconds", "rays")}
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default=None)
+    args = ap.parse_args()
+    global WORKLOAD
+    if args.workload:
+        WORKLOAD = args.workload
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

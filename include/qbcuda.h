@@ -1,0 +1,260 @@
+/*
+ * libqbcuda — GB300 (sm_103a) implementation of qubatron's octree ray-cast
+ * path behind a plain C ABI.
+ *
+ * It replaces the GL connector of the reference, src/qubatron/octree_glc.c
+ * (interface at octree_glc.c:65-85): the same buffers are uploaded with the
+ * same (data, type, size, itemsize, start, end, buftype) arguments, and one
+ * render call draws a frame the way octree_glc_update does, into a headless
+ * RGBA buffer instead of a GL framebuffer. The per-pixel work is the fragment
+ * shader src/qubatron/shaders/octree_fsh.c (primary ray, shadow ray, shading,
+ * light flare), reproduced bit for bit in FP32.
+ *
+ * Conventions
+ *  - Every call returns 0 on success or a negative QBC_E_* code; the message
+ *    of the last failure on the calling thread is qbc_last_error().
+ *  - One context drives one GPU and is not thread-safe, like the single GL
+ *    context of the reference.
+ *  - Output rows run bottom-up (row 0 is the bottom row), as glReadPixels
+ *    returns a GL framebuffer.
+ */
+#ifndef QBCUDA_H
+#define QBCUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- error codes ---- */
+#define QBC_OK 0
+#define QBC_E_ARG -1      /* bad argument (range, itemsize, type, size) */
+#define QBC_E_CUDA -2     /* a CUDA runtime call failed */
+#define QBC_E_NOMEM -3    /* device or host allocation failed */
+#define QBC_E_STATE -4    /* call not valid in this state */
+#define QBC_E_TIMEOUT -5  /* a bounded wait inside a kernel gave up */
+
+/* ---- GL enums the reference passes as `type` (GL/gl.h values) ---- */
+#define QBC_GL_INT 0x1404
+#define QBC_GL_FLOAT 0x1406
+
+/* Buffer ids: same order and meaning as octree_glc_buffer_t (octree_glc.c:16-24). */
+typedef enum qbc_buffer
+{
+    QBC_STATIC_COLOR   = 0,
+    QBC_STATIC_NORMAL  = 1,
+    QBC_STATIC_OCTREE  = 2,
+    QBC_DYNAMIC_COLOR  = 3,
+    QBC_DYNAMIC_NORMAL = 4,
+    QBC_DYNAMIC_OCTREE = 5
+} qbc_buffer;
+
+typedef struct qbc_ctx qbc_ctx;
+
+/*
+ * Uniforms of one frame. qbc_view_setup derives them from the arguments of
+ * octree_glc_update (octree_glc.c:263-284) and from the frame-constant part of
+ * the shader's main() (octree_fsh.c:401-418); everything per pixel is done on
+ * the GPU. Filling the struct directly renders with exactly these values.
+ */
+typedef struct qbc_view
+{
+    float   camfp[3];       /* camera position (uniform camfp) */
+    float   light[3];       /* uniform light */
+    float   basecube[4];    /* (0, S, S, S) */
+    float   dim[2];         /* uniform dimensions: (ow, oh) */
+    float   cfp[3];         /* screen-space focus point (ow/2, oh/2, focal) */
+    float   qz[4];          /* yaw quaternion, about +y by -angle.x */
+    float   qx[4];          /* pitch quaternion, about the rotated -x by -angle.y */
+    float   ncamlight[3];   /* normalize(light - camfp) */
+    float   flare_cos;      /* largest float <= cos(0.02f): camangle < 0.02 test */
+    float   coord_scale[2]; /* ow / width_px, oh / height_px (1.0 for whole sizes) */
+    int32_t width_px;       /* (int) ow: the GL viewport width */
+    int32_t height_px;
+    int32_t maxlevel;       /* uniform maxlevel, 0..QBC_MAX_LEVEL */
+    int32_t shoot;          /* uniform shoot */
+} qbc_view;
+
+#define QBC_MAX_LEVEL 17 /* the shader's stack holds 18 levels (octree_fsh.c:151) */
+
+/* Per-pixel status bits (qbc_outputs.flags). */
+#define QBC_PX_PRIMARY_LEAF (1u << 0) /* primary ray reached a leaf */
+#define QBC_PX_DISCARD (1u << 1)      /* a traversal discarded the fragment: pixel left at 0 */
+#define QBC_PX_SHADED (1u << 2)       /* res.isp.w > 0: shadow ray traced and pixel shaded */
+#define QBC_PX_SHADOW_LEAF (1u << 3)  /* shadow ray reached a leaf */
+#define QBC_PX_LIT (1u << 4)          /* step(sqr, 15.0) == 1 */
+#define QBC_PX_FLARE_TEST (1u << 5)   /* camangle < 0.02: flare ray traced */
+#define QBC_PX_FLARE_WHITE (1u << 6)  /* flare turned the pixel white */
+#define QBC_PX_OOB (1u << 7)          /* a node or point index fell outside the uploaded arrays */
+
+/*
+ * Output buffers of one view; any pointer may be NULL. All are width_px *
+ * height_px pixels, row 0 at the bottom.
+ *   rgba8   4 bytes per pixel, the RGBA8 target of the reference (octree_glc.c:237)
+ *   rgba32f 4 floats per pixel, the fragment colour before quantisation
+ *   flags   QBC_PX_* bits
+ *   leaf    4 int32 per pixel: primary leaf node (static, dynamic), shadow
+ *           leaf node (static, dynamic); -1 where no leaf was reached
+ *   isp     4 floats per pixel: primary intersection (x, y, z, t)
+ *   visits  4 uint32 per pixel: node visits of the primary ray (static,
+ *           dynamic) and of the shadow ray (static, dynamic)
+ */
+typedef struct qbc_outputs
+{
+    uint8_t*  rgba8;
+    float*    rgba32f;
+    uint32_t* flags;
+    int32_t*  leaf;
+    float*    isp;
+    uint32_t* visits;
+} qbc_outputs;
+
+/* Library version string. */
+const char* qbc_version(void);
+
+/* Message of the last failed call on this thread ("" when none). */
+const char* qbc_last_error(void);
+
+/*
+ * Create a context on CUDA device `device` (replaces octree_glc_init,
+ * octree_glc.c:93-247: no shaders to compile, six empty buffers).
+ */
+int qbc_create(int device, qbc_ctx** out);
+int qbc_destroy(qbc_ctx* ctx);
+
+/*
+ * Upload a range of a host buffer (replaces octree_glc_upload_texbuffer_data,
+ * octree_glc.c:361-498), same argument meaning:
+ *   data      base of the WHOLE host array (the copy reads data + start)
+ *   type      QBC_GL_FLOAT for colour/normal, QBC_GL_INT for octrees
+ *   size      bytes of the whole array; the device buffer grows to hold it and
+ *             is then refilled from [0, size), as the reference re-creates its
+ *             texture (octree_glc.c:412-428)
+ *   itemsize  12 (one float3 point) for colour/normal; 16 (one RGBA32I texel,
+ *             3 per node) or 48 (one node) for octrees
+ *   start,end byte range [start, end) to copy; an octree range is widened to
+ *             whole nodes [start/48, ceil(end/48))
+ * Octree nodes (12 int32: 8 children, model index, 3 pad; octree.c:11-14) are
+ * repacked on the device into 32-byte child blocks plus a model-index array.
+ * The host array may be reused as soon as the call returns.
+ */
+int qbc_upload(qbc_ctx* ctx, const void* data, int type, size_t size, size_t itemsize, size_t start, size_t end, int buftype);
+
+/*
+ * Derive the uniforms of one frame from the arguments of octree_glc_update
+ * (octree_glc.c:249-284). focal <= 0 selects the reference's focal length
+ * (ow/2)/tan(pi/4) (octree_fsh.c:403); a positive value sets cfp.z directly.
+ */
+int qbc_view_setup(float width, float height, const float position[3], const float angle[3], float lighta, int quality, int maxlevel, float basesize, int shoot, float focal, qbc_view* out);
+
+/*
+ * Render one frame with the reference's arguments (replaces
+ * octree_glc_update, octree_glc.c:249-352, without the window blit):
+ * width_px x height_px RGBA8 pixels into the host buffer rgba8_out. Blocks
+ * until the pixels are in host memory.
+ */
+int qbc_render(qbc_ctx* ctx, float width, float height, const float position[3], const float angle[3], float lighta, int quality, int maxlevel, float basesize, int shoot, uint8_t* rgba8_out);
+
+/*
+ * Render n views in one batch. outs[i] holds the outputs of views[i]; the
+ * pointers are host memory when outputs_on_device is 0 (pinned memory gives
+ * the fastest copy) and device memory of this context's GPU otherwise. With
+ * device outputs the call returns once the work is queued on the context's
+ * stream; with host outputs it returns when the pixels are on the host.
+ */
+int qbc_render_views(qbc_ctx* ctx, const qbc_view* views, const qbc_outputs* outs, int n, int outputs_on_device);
+
+/*
+ * Batched ray queries through the same traversal (cube_trace_line,
+ * octree_fsh.c:138-379): the reference's CPU callers of octree_trace_line
+ * (qubatron.c:214-240, zombie.c:296-486) and the particle collision shader
+ * (particle_vsh.c:122-374) ask exactly this. Per ray i, any pointer may be NULL:
+ *   status  0 miss, 1 leaf reached, 2 discarded (fewer than 2 basecube faces)
+ *   leaf    2 int32: node index at the leaf (static, dynamic), -1 when none
+ *   model   2 int32: slot-8 model index at the leaf (static, dynamic)
+ *   isp     4 floats: entry point of the leaf cell (x, y, z, t)
+ *   col,nrm 4 floats each: colour and normal the shader fetches at the leaf
+ *   visits  2 uint32: node visits (static, dynamic)
+ * pos and dir are n float3; all arrays are host memory when on_device is 0,
+ * device memory otherwise.
+ */
+typedef struct qbc_ray_hits
+{
+    int32_t*  status;
+    int32_t*  leaf;
+    int32_t*  model;
+    float*    isp;
+    float*    col;
+    float*    nrm;
+    uint32_t* visits;
+} qbc_ray_hits;
+
+int qbc_trace_rays(qbc_ctx* ctx, const float* pos, const float* dir, int64_t n, const float basecube[4], int maxlevel, const qbc_ray_hits* out, int on_device);
+
+/* Run the context's work on this CUDA stream (a cudaStream_t; NULL = the
+ * context's own stream). */
+int qbc_set_stream(qbc_ctx* ctx, void* stream);
+int qbc_synchronize(qbc_ctx* ctx);
+
+/* Node and point counts currently held for a tree / model (0 static, 1 dynamic). */
+int qbc_tree_nodes(qbc_ctx* ctx, int tree, int64_t* n_nodes);
+int qbc_model_points(qbc_ctx* ctx, int model, int64_t* n_points);
+
+/* Kernel launches issued by this context since creation. */
+int qbc_launch_count(qbc_ctx* ctx, int64_t* count);
+
+/* ---- node-array producer (octree.c:95-218) ---- */
+
+/* A growable host node array (12 int32 per node, node 0 = root). */
+typedef struct qbc_octree qbc_octree;
+
+/* New tree holding only the root (octree_create, octree.c:55-67). */
+int qbc_octree_create(float basesize, int levels, qbc_octree** out);
+int qbc_octree_free(qbc_octree* tree);
+/* Back to the root alone (octree_reset, octree.c:89-93). */
+int qbc_octree_reset(qbc_octree* tree);
+/* octree_insert_point (octree.c:95-147) for n points in order, model indices
+ * first_index + i. */
+int qbc_octree_insert_points(qbc_octree* tree, const float* pnts, int64_t n, int64_t first_index);
+/* octree_insert_path (octree.c:149-180): octets holds `levels` octets per point. */
+int qbc_octree_insert_paths(qbc_octree* tree, const int32_t* octets, int64_t n, int64_t first_index);
+/* octree_remove_point (octree.c:182-218). */
+int qbc_octree_remove_point(qbc_octree* tree, const float pnt[3], int32_t* modind, int32_t* octind);
+/* Node array and node count (valid until the tree changes). */
+int qbc_octree_nodes(qbc_octree* tree, const int32_t** nodes, int64_t* n_nodes);
+
+/* ---- seeded synthetic scenes ---- */
+
+#define QBC_SCENE_FLOOR 0 /* floor plane + boxes + spheres */
+#define QBC_SCENE_ROOM 1  /* closed room (floor, 4 walls, ceiling) + boxes + spheres */
+
+typedef struct qbc_scene_desc
+{
+    int32_t  kind;
+    int32_t  levels;
+    int64_t  n_points;
+    uint64_t seed;
+    float    basesize;
+    int32_t  n_boxes;
+    float    box_min, box_max;
+    int32_t  n_spheres;
+    float    sphere_min, sphere_max;
+    float    color_noise; /* uniform +- per channel around the primitive colour */
+} qbc_scene_desc;
+
+/*
+ * Generate n_points float3 points, normals and colours. Points are emitted in
+ * octree-path order (a stable sort by the 3-bit octets of octree.c:100-109,
+ * root first), the order a voxel-sorted asset has, so that inserting them in
+ * order builds the tree front to back. Only +, -, *, / and sqrt are used, so
+ * every machine generates the same bits.
+ */
+int qbc_scene_generate(const qbc_scene_desc* desc, float* pnts, float* nrms, float* cols);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,77 @@
+/*
+ * Flat entry points over the reference's own src/qubatron/octree.c, compiled
+ * from the reference sources by oracle/build_ref.sh into oracle/_ref. Test
+ * infrastructure only: it pins the oracle's restatement (qbo_octree.c,
+ * qbo_trace.c) to the reference's CPU insertion and static-tree traversal.
+ */
+#include "octree.c" /* declarations only: included below level 0 */
+
+#include <string.h>
+
+/* Build a static tree with octree_insert_point (octree.c:95-147) for points in
+ * order; returns the node count, copying nodes into out when they fit. */
+long qbref_build(const float* pts, long n, float basesize, int levels, int* out, long cap)
+{
+    octree_t tree = octree_create((v4_t){0.0f, basesize, basesize, basesize}, levels);
+    for (long i = 0; i < n; i++)
+        octree_insert_point(&tree, 0, (size_t) i, (v3_t){pts[i * 3 + 0], pts[i * 3 + 1], pts[i * 3 + 2]}, NULL);
+    long len = (long) tree.len;
+    if (out != NULL && len <= cap) memcpy(out, tree.octs, (size_t) len * sizeof(octets_t));
+    octree_delete(&tree);
+    return len;
+}
+
+/* Build with octree_insert_path (octree.c:149-180) from per-point octets
+ * (levels <= 12, one row of 12 per point). */
+long qbref_build_paths(const int* octets, long n, float basesize, int levels, int* out, long cap)
+{
+    octree_t tree = octree_create((v4_t){0.0f, basesize, basesize, basesize}, levels);
+    for (long i = 0; i < n; i++)
+    {
+        int o14[4], o54[4], o94[4];
+        for (int k = 0; k < 4; k++)
+        {
+            o14[k] = octets[i * 12 + k];
+            o54[k] = octets[i * 12 + 4 + k];
+            o94[k] = octets[i * 12 + 8 + k];
+        }
+        octree_insert_path(&tree, 0, (size_t) i, o14, o54, o94);
+    }
+    long len = (long) tree.len;
+    if (out != NULL && len <= cap) memcpy(out, tree.octs, (size_t) len * sizeof(octets_t));
+    octree_delete(&tree);
+    return len;
+}
+
+/* octree_remove_point (octree.c:182-218) on a caller-owned node array. */
+void qbref_remove(int* nodes, long n_nodes, float basesize, int levels, const float* pnt, int* modind, int* octind)
+{
+    octree_t tree;
+    tree.basecube = (v4_t){0.0f, basesize, basesize, basesize};
+    tree.octs     = (octets_t*) nodes;
+    tree.size     = (size_t) n_nodes;
+    tree.len      = (size_t) n_nodes;
+    tree.levels   = levels;
+    octree_remove_point(&tree, (v3_t){pnt[0], pnt[1], pnt[2]}, modind, octind);
+}
+
+/* octree_trace_line (octree.c:341-537) for n rays; out_tlf gets the leaf cube,
+ * w = -1 when no leaf was reached. */
+void qbref_trace(const int* nodes, long n_nodes, float basesize, int levels, const float* pos, const float* dir, long n, int* out_model, float* out_tlf)
+{
+    octree_t tree;
+    tree.basecube = (v4_t){0.0f, basesize, basesize, basesize};
+    tree.octs     = (octets_t*) nodes;
+    tree.size     = (size_t) n_nodes;
+    tree.len      = (size_t) n_nodes;
+    tree.levels   = levels;
+    for (long i = 0; i < n; i++)
+    {
+        v4_t tlf       = {0.0f, 0.0f, 0.0f, -1.0f};
+        out_model[i]   = octree_trace_line(&tree, (v3_t){pos[i * 3], pos[i * 3 + 1], pos[i * 3 + 2]}, (v3_t){dir[i * 3], dir[i * 3 + 1], dir[i * 3 + 2]}, &tlf);
+        out_tlf[i * 4 + 0] = tlf.x;
+        out_tlf[i * 4 + 1] = tlf.y;
+        out_tlf[i * 4 + 2] = tlf.z;
+        out_tlf[i * 4 + 3] = tlf.w;
+    }
+}

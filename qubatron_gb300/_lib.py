@@ -1,0 +1,179 @@
+"""ctypes binding of libqbcuda (include/qbcuda.h).
+
+The library is the product; this module only declares its C signatures and
+turns a negative status into QbcError. There is no fallback: if the shared
+library is missing or fails to load, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+c_float_p = C.POINTER(C.c_float)
+c_int32_p = C.POINTER(C.c_int32)
+c_int64_p = C.POINTER(C.c_int64)
+
+QBC_GL_INT = 0x1404
+QBC_GL_FLOAT = 0x1406
+
+STATIC_COLOR, STATIC_NORMAL, STATIC_OCTREE, DYNAMIC_COLOR, DYNAMIC_NORMAL, DYNAMIC_OCTREE = range(6)
+MAX_LEVEL = 17
+
+PX_PRIMARY_LEAF = 1 << 0
+PX_DISCARD = 1 << 1
+PX_SHADED = 1 << 2
+PX_SHADOW_LEAF = 1 << 3
+PX_LIT = 1 << 4
+PX_FLARE_TEST = 1 << 5
+PX_FLARE_WHITE = 1 << 6
+PX_OOB = 1 << 7
+
+SCENE_FLOOR = 0
+SCENE_ROOM = 1
+
+ERRORS = {-1: "QBC_E_ARG", -2: "QBC_E_CUDA", -3: "QBC_E_NOMEM", -4: "QBC_E_STATE", -5: "QBC_E_TIMEOUT"}
+
+
+class QbcError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class View(C.Structure):
+    """qbc_view: the uniforms of one frame."""
+
+    _fields_ = [
+        ("camfp", C.c_float * 3),
+        ("light", C.c_float * 3),
+        ("basecube", C.c_float * 4),
+        ("dim", C.c_float * 2),
+        ("cfp", C.c_float * 3),
+        ("qz", C.c_float * 4),
+        ("qx", C.c_float * 4),
+        ("ncamlight", C.c_float * 3),
+        ("flare_cos", C.c_float),
+        ("coord_scale", C.c_float * 2),
+        ("width_px", C.c_int32),
+        ("height_px", C.c_int32),
+        ("maxlevel", C.c_int32),
+        ("shoot", C.c_int32),
+    ]
+
+    def to_bytes(self) -> bytes:
+        return bytes(memoryview(self).cast("B"))
+
+    @classmethod
+    def from_bytes(cls, b: bytes) -> "View":
+        v = cls()
+        C.memmove(C.addressof(v), b, C.sizeof(cls))
+        return v
+
+
+class Outputs(C.Structure):
+    """qbc_outputs: per-view output pointers (host or device)."""
+
+    _fields_ = [
+        ("rgba8", C.c_void_p),
+        ("rgba32f", C.c_void_p),
+        ("flags", C.c_void_p),
+        ("leaf", C.c_void_p),
+        ("isp", C.c_void_p),
+        ("visits", C.c_void_p),
+    ]
+
+
+class RayHits(C.Structure):
+    """qbc_ray_hits: per-ray output pointers (host or device)."""
+
+    _fields_ = [
+        ("status", C.c_void_p),
+        ("leaf", C.c_void_p),
+        ("model", C.c_void_p),
+        ("isp", C.c_void_p),
+        ("col", C.c_void_p),
+        ("nrm", C.c_void_p),
+        ("visits", C.c_void_p),
+    ]
+
+
+class SceneDesc(C.Structure):
+    """qbc_scene_desc."""
+
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("levels", C.c_int32),
+        ("n_points", C.c_int64),
+        ("seed", C.c_uint64),
+        ("basesize", C.c_float),
+        ("n_boxes", C.c_int32),
+        ("box_min", C.c_float),
+        ("box_max", C.c_float),
+        ("n_spheres", C.c_int32),
+        ("sphere_min", C.c_float),
+        ("sphere_max", C.c_float),
+        ("color_noise", C.c_float),
+    ]
+
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "qbc_version": (C.c_char_p, []),
+    "qbc_last_error": (C.c_char_p, []),
+    "qbc_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
+    "qbc_destroy": (C.c_int, [C.c_void_p]),
+    "qbc_upload": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_size_t, C.c_size_t, C.c_size_t, C.c_size_t, C.c_int]),
+    "qbc_view_setup": (C.c_int, [C.c_float, C.c_float, c_float_p, c_float_p, C.c_float, C.c_int, C.c_int,
+                                 C.c_float, C.c_int, C.c_float, C.POINTER(View)]),
+    "qbc_render": (C.c_int, [C.c_void_p, C.c_float, C.c_float, c_float_p, c_float_p, C.c_float, C.c_int, C.c_int,
+                             C.c_float, C.c_int, C.c_void_p]),
+    "qbc_render_views": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int, C.c_int]),
+    "qbc_trace_rays": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, c_float_p, C.c_int,
+                                 C.POINTER(RayHits), C.c_int]),
+    "qbc_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "qbc_synchronize": (C.c_int, [C.c_void_p]),
+    "qbc_tree_nodes": (C.c_int, [C.c_void_p, C.c_int, c_int64_p]),
+    "qbc_model_points": (C.c_int, [C.c_void_p, C.c_int, c_int64_p]),
+    "qbc_launch_count": (C.c_int, [C.c_void_p, c_int64_p]),
+    "qbc_octree_create": (C.c_int, [C.c_float, C.c_int, C.POINTER(C.c_void_p)]),
+    "qbc_octree_free": (C.c_int, [C.c_void_p]),
+    "qbc_octree_reset": (C.c_int, [C.c_void_p]),
+    "qbc_octree_insert_points": (C.c_int, [C.c_void_p, c_float_p, C.c_int64, C.c_int64]),
+    "qbc_octree_insert_paths": (C.c_int, [C.c_void_p, c_int32_p, C.c_int64, C.c_int64]),
+    "qbc_octree_remove_point": (C.c_int, [C.c_void_p, c_float_p, c_int32_p, c_int32_p]),
+    "qbc_octree_nodes": (C.c_int, [C.c_void_p, C.POINTER(c_int32_p), c_int64_p]),
+    "qbc_scene_generate": (C.c_int, [C.POINTER(SceneDesc), c_float_p, c_float_p, c_float_p]),
+}
+
+_LIB = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True) -> C.CDLL:
+    """Load libqbcuda.so (building it first if asked); raise if unavailable."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = lib_path()
+    if build_if_missing:
+        _build.build()
+    if not os.path.exists(path):
+        raise QbcError(-4, f"libqbcuda.so not built at {path}")
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def check(rc: int) -> None:
+    if rc != 0:
+        msg = _LIB.qbc_last_error().decode() if _LIB is not None else ""
+        raise QbcError(rc, msg)

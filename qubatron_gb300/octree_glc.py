@@ -1,0 +1,208 @@
+"""Host-side mirror of the reference's GL connector for the octree ray-cast
+path (src/qubatron/octree_glc.c:65-85), running on libqbcuda.
+
+Names and argument meanings follow the reference:
+
+* ``octree_glc_init(path)``                       -> octree_glc.c:93-247
+* ``octree_glc_upload_texbuffer_data(rc, data, type, size, itemsize, start, end, buftype)``
+                                                  -> octree_glc.c:361-498
+* ``octree_glc_update(rc, width, height, position, angle, lighta, quality, maxlevel, basesize, shoot)``
+                                                  -> octree_glc.c:249-352
+
+Differences, all deliberate: there is no window, so ``octree_glc_update``
+returns the RGBA8 render target as an (oh, ow, 4) uint8 array with row 0 at
+the bottom instead of blitting it; failures raise QbcError where the
+reference silently ignores GL errors.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Iterable, Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import Outputs, QbcError, View, check
+
+GL_INT = _lib.QBC_GL_INT
+GL_FLOAT = _lib.QBC_GL_FLOAT
+
+OCTREE_GLC_BUFFER_STATIC_COLOR = _lib.STATIC_COLOR
+OCTREE_GLC_BUFFER_STATIC_NORMAL = _lib.STATIC_NORMAL
+OCTREE_GLC_BUFFER_STATIC_OCTREE = _lib.STATIC_OCTREE
+OCTREE_GLC_BUFFER_DYNAMIC_COLOR = _lib.DYNAMIC_COLOR
+OCTREE_GLC_BUFFER_DYNAMIC_NORMAL = _lib.DYNAMIC_NORMAL
+OCTREE_GLC_BUFFER_DYNAMIC_OCTREE = _lib.DYNAMIC_OCTREE
+
+
+def _f3(v) -> C.Array:
+    a = (C.c_float * 3)()
+    for k in range(3):
+        a[k] = float(v[k])
+    return a
+
+
+def view_setup(width: float, height: float, position, angle, lighta: float, quality: int, maxlevel: int,
+               basesize: float, shoot: int = 0, focal: float = 0.0) -> View:
+    """Uniforms of one frame (qbc_view_setup)."""
+    lib = _lib.load()
+    v = View()
+    check(lib.qbc_view_setup(width, height, _f3(position), _f3(angle), lighta, int(quality), int(maxlevel),
+                             basesize, int(shoot), focal, C.byref(v)))
+    return v
+
+
+class FrameBuffers:
+    """Host (numpy) outputs for one view; pass names of the streams wanted."""
+
+    SHAPES = {"rgba8": (4, np.uint8), "rgba32f": (4, np.float32), "flags": (1, np.uint32),
+              "leaf": (4, np.int32), "isp": (4, np.float32), "visits": (4, np.uint32)}
+
+    def __init__(self, view: View, streams: Iterable[str] = ("rgba8",)):
+        h, w = view.height_px, view.width_px
+        self.arrays = {}
+        for s in streams:
+            comps, dt = self.SHAPES[s]
+            shape = (h, w) if comps == 1 else (h, w, comps)
+            self.arrays[s] = np.zeros(shape, dtype=dt)
+
+    def outputs(self) -> Outputs:
+        o = Outputs()
+        for s, a in self.arrays.items():
+            setattr(o, s, a.ctypes.data)
+        return o
+
+    def __getitem__(self, k: str) -> np.ndarray:
+        return self.arrays[k]
+
+
+class OctreeGLC:
+    """octree_glc_t: one libqbcuda context on one GPU."""
+
+    def __init__(self, device: int = 0):
+        self._lib = _lib.load()
+        h = C.c_void_p()
+        check(self._lib.qbc_create(int(device), C.byref(h)))
+        self.handle = h
+
+    def close(self) -> None:
+        if self.handle:
+            self._lib.qbc_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---- octree_glc_upload_texbuffer_data ----
+    def upload_texbuffer_data(self, data, type: int, size: int, itemsize: int, start: int, end: int,
+                              buftype: int) -> None:
+        """`data` is the whole host array (a C-contiguous numpy array or an int
+        address); the copy reads bytes [start, end) of it."""
+        if isinstance(data, np.ndarray):
+            if not data.flags.c_contiguous:
+                raise QbcError(-1, "upload data must be C-contiguous")
+            if data.nbytes < size:
+                raise QbcError(-1, f"upload size {size} exceeds the array's {data.nbytes} bytes")
+            ptr = data.ctypes.data
+        else:
+            ptr = int(data)
+        check(self._lib.qbc_upload(self.handle, C.c_void_p(ptr), int(type), int(size), int(itemsize), int(start),
+                                   int(end), int(buftype)))
+
+    # ---- octree_glc_update ----
+    def update(self, width: float, height: float, position, angle, lighta: float, quality: int, maxlevel: int,
+               basesize: float, shoot: int = 0) -> np.ndarray:
+        v = view_setup(width, height, position, angle, lighta, quality, maxlevel, basesize, shoot)
+        out = np.zeros((v.height_px, v.width_px, 4), dtype=np.uint8)
+        check(self._lib.qbc_render(self.handle, width, height, _f3(position), _f3(angle), lighta, int(quality),
+                                   int(maxlevel), basesize, int(shoot), C.c_void_p(out.ctypes.data)))
+        return out
+
+    def render_views(self, views: Sequence[View], outputs: Sequence[Outputs], on_device: bool) -> None:
+        n = len(views)
+        varr = (View * n)(*views)
+        oarr = (Outputs * n)(*outputs)
+        check(self._lib.qbc_render_views(self.handle, varr, oarr, n, 1 if on_device else 0))
+
+    def render_host(self, views: Sequence[View], streams: Iterable[str] = ("rgba8",)) -> list:
+        """Render views into fresh numpy buffers; returns a FrameBuffers per view."""
+        bufs = [FrameBuffers(v, streams) for v in views]
+        self.render_views(views, [b.outputs() for b in bufs], on_device=False)
+        return bufs
+
+    def trace_rays(self, pos: np.ndarray, dirs: np.ndarray, basecube, maxlevel: int) -> dict:
+        """Batched ray queries (qbc_trace_rays) on host arrays -> dict of arrays."""
+        pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+        dirs = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+        n = pos.shape[0]
+        out = {"status": np.zeros(n, np.int32), "leaf": np.zeros((n, 2), np.int32),
+               "model": np.zeros((n, 2), np.int32), "isp": np.zeros((n, 4), np.float32),
+               "col": np.zeros((n, 4), np.float32), "nrm": np.zeros((n, 4), np.float32),
+               "visits": np.zeros((n, 2), np.uint32)}
+        h = _lib.RayHits(*[out[k].ctypes.data for k in ("status", "leaf", "model", "isp", "col", "nrm", "visits")])
+        bc = (C.c_float * 4)(*[float(x) for x in basecube])
+        check(self._lib.qbc_trace_rays(self.handle, C.c_void_p(pos.ctypes.data), C.c_void_p(dirs.ctypes.data), n, bc,
+                                       int(maxlevel), C.byref(h), 0))
+        return out
+
+    def set_stream(self, stream_ptr: Optional[int]) -> None:
+        check(self._lib.qbc_set_stream(self.handle, C.c_void_p(stream_ptr or 0)))
+
+    def synchronize(self) -> None:
+        check(self._lib.qbc_synchronize(self.handle))
+
+    def tree_nodes(self, tree: int) -> int:
+        n = C.c_int64()
+        check(self._lib.qbc_tree_nodes(self.handle, tree, C.byref(n)))
+        return n.value
+
+    def model_points(self, model: int) -> int:
+        n = C.c_int64()
+        check(self._lib.qbc_model_points(self.handle, model, C.byref(n)))
+        return n.value
+
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        check(self._lib.qbc_launch_count(self.handle, C.byref(n)))
+        return n.value
+
+    # convenience: whole-array uploads in the reference's call pattern
+    def upload_model(self, dynamic: bool, colors: np.ndarray, normals: np.ndarray) -> None:
+        colors = np.ascontiguousarray(colors, dtype=np.float32)
+        normals = np.ascontiguousarray(normals, dtype=np.float32)
+        base = DYNAMIC if dynamic else STATIC
+        self.upload_texbuffer_data(colors, GL_FLOAT, colors.nbytes, 12, 0, colors.nbytes, base + 0)
+        self.upload_texbuffer_data(normals, GL_FLOAT, normals.nbytes, 12, 0, normals.nbytes, base + 1)
+
+    def upload_octree(self, dynamic: bool, nodes: np.ndarray) -> None:
+        nodes = np.ascontiguousarray(nodes, dtype=np.int32)
+        base = DYNAMIC if dynamic else STATIC
+        self.upload_texbuffer_data(nodes, GL_INT, nodes.nbytes, 16, 0, nodes.nbytes, base + 2)
+
+
+STATIC = 0
+DYNAMIC = 3
+
+
+def octree_glc_init(path: Optional[str] = None, device: int = 0) -> OctreeGLC:
+    """octree_glc_init: `path` (the shader directory) is accepted and unused."""
+    return OctreeGLC(device)
+
+
+def octree_glc_upload_texbuffer_data(rc: OctreeGLC, data, type: int, size: int, itemsize: int, start: int,
+                                     end: int, buftype: int) -> None:
+    rc.upload_texbuffer_data(data, type, size, itemsize, start, end, buftype)
+
+
+def octree_glc_update(rc: OctreeGLC, width: float, height: float, position, angle, lighta: float, quality: int,
+                      maxlevel: int, basesize: float, shoot: int = 0) -> np.ndarray:
+    return rc.update(width, height, position, angle, lighta, quality, maxlevel, basesize, shoot)

@@ -1,0 +1,151 @@
+"""Generate the golden fixtures in tests/golden from the reference itself.
+
+Run in a checkout that has the reference sources (default /root/reference):
+
+    python tests/golden/make_golden.py [REFERENCE_ROOT]
+
+It compiles the reference's src/qubatron/octree.c (oracle/build_ref.sh) and
+records what that code produces:
+
+* ``five_point.npz``   the 5-point OCTTEST scene of modelutil.c:91-129:
+                       node array from octree_insert_point, and
+                       octree_trace_line results for an edge-case ray suite;
+* ``floor50k.npz``     a 50,000-point seeded floor scene: node count and
+                       SHA-256 of the node array from octree_insert_point, node
+                       array from octree_insert_path over the same octets,
+                       octree_remove_point results, and octree_trace_line
+                       results for random and edge-case rays.
+
+octree_trace_line covers the static single-tree traversal; rays on which
+more than 4 basecube faces pass the entry test overflow the reference's
+hitp[4] array (undefined behaviour) and are left out.
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import qbo  # noqa: E402
+
+S = 1800.0
+LEVELS = 12
+FIVE_POINTS = np.array([[10, 690, 10], [10, 340, 10], [10, 340, 690], [10, 10, 10], [690, 10, 690]], np.float32)
+
+
+def edge_rays(points: np.ndarray, seed: int, n_aim: int = 600):
+    """Rays that stress the traversal's tie rules: axis-parallel directions,
+    cameras on bisecting planes, cell edges and corners, inside and outside
+    the basecube, rays aimed exactly at points and at cell boundaries."""
+    rng = np.random.default_rng(seed)
+    cams = [
+        (900.0, 900.0, 3000.0),   # OCTTEST camera (qubatron.c:136), outside the cube
+        (700.0, 150.0, 350.0),    # default start (qubatron.c:580)
+        (900.0, 420.0, 1700.0),   # on the level-0 x bisecting plane
+        (900.0, 900.0, 900.0),    # centre: on all three level-0 planes
+        (450.0, 450.0, 450.0),    # a level-1 cell centre
+        (0.0, 900.0, 900.0),      # on the left face
+        (1800.0, 0.0, 0.0),       # the one corner inside every half-open test
+        (10.0, 690.0, 10.0),      # on a point
+        (-300.0, 700.0, 900.0),   # outside, left
+        (903.7, 421.3, 1702.9),   # generic inside
+        (2500.0, 2500.0, 2500.0), # outside, far corner
+    ]
+    dirs_axis = [(1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1), (1, 1, 0), (1, -1, 1),
+                 (-1, -1, -1), (0, 1, 1), (1, 0, -1), (0.5, -0.25, -1.0), (0, 0, 0)]
+    pos, dirs = [], []
+    for c in cams:
+        for d in dirs_axis:
+            pos.append(c)
+            dirs.append(d)
+        for k in range(n_aim // len(cams)):
+            tgt = points[rng.integers(0, len(points))].astype(np.float64)
+            mode = k % 4
+            if mode == 1:   # cell corner of the target's leaf
+                w = S / 4096.0
+                tgt = np.floor(tgt / w) * w
+            elif mode == 2:  # slightly off the point
+                tgt = tgt + rng.normal(0, 0.3, 3)
+            elif mode == 3:  # a bisecting plane coordinate on one axis
+                ax = rng.integers(0, 3)
+                lvl = rng.integers(1, LEVELS)
+                w = S / (2.0 ** lvl)
+                tgt[ax] = np.round(tgt[ax] / w) * w
+            pos.append(c)
+            dirs.append(tuple(tgt - np.array(c)))
+    return np.array(pos, np.float32), np.array(dirs, np.float32)
+
+
+def random_rays(points: np.ndarray, seed: int, n: int):
+    rng = np.random.default_rng(seed)
+    pos = rng.uniform(-400.0, 2200.0, (n, 3)).astype(np.float32)
+    tgt = points[rng.integers(0, len(points), n)] + rng.normal(0, 1.5, (n, 3)).astype(np.float32)
+    return pos, (tgt - pos).astype(np.float32)
+
+
+def keep_defined(scene: qbo.Scene, pos, dirs):
+    """Drop rays on which more than 4 basecube faces pass (hitp[4] overflow)."""
+    keep = np.array([qbo.trace(scene, (0.0, S, S, S), LEVELS, p, d).faces <= 4 for p, d in zip(pos, dirs)])
+    return pos[keep], dirs[keep]
+
+
+def floor_points(n: int):
+    from qubatron_gb300 import scenes
+    pts, nrm, col = scenes.generate_points(scenes.scaled_spec("floor1m", n))
+    return pts, nrm, col
+
+
+def main(root: str) -> None:
+    if qbo.build_reference(root) is None:
+        raise SystemExit(f"reference sources not found under {root}")
+
+    # ---- 5-point scene ----
+    nodes5 = qbo.ref_build(FIVE_POINTS, S, LEVELS)
+    sc5 = qbo.Scene(nodes5, np.ones((5, 3), np.float32), np.tile([0, 0, -1], (5, 1)).astype(np.float32))
+    pos, dirs = keep_defined(sc5, *edge_rays(FIVE_POINTS, 11))
+    model, tlf = qbo.ref_trace(nodes5, S, LEVELS, pos, dirs)
+    np.savez_compressed(os.path.join(HERE, "five_point.npz"), points=FIVE_POINTS, nodes=nodes5, ray_pos=pos,
+                        ray_dir=dirs, ref_model=model, ref_tlf=tlf)
+    print("five_point:", nodes5.shape[0], "nodes,", len(pos), "rays,", int((tlf[:, 3] >= 0).sum()), "leaf hits")
+
+    # ---- seeded floor scene ----
+    pts, nrm, col = floor_points(50_000)
+    nodes = qbo.ref_build(pts, S, LEVELS)
+    octets = qbo.point_octets(pts, S, LEVELS)
+    nodes_path = qbo.ref_build_paths(octets, S, LEVELS)
+    sc = qbo.Scene(nodes, col, nrm)
+    ep, ed = keep_defined(sc, *edge_rays(pts, 12))
+    rp, rd = keep_defined(sc, *random_rays(pts, 13, 3000))
+    pos = np.concatenate([ep, rp])
+    dirs = np.concatenate([ed, rd])
+    model, tlf = qbo.ref_trace(nodes, S, LEVELS, pos, dirs)
+    # octree_remove_point on a copy, for 64 points
+    rm = nodes.copy()
+    lib = qbo.ref()
+    idx = np.random.default_rng(14).choice(len(pts), 64, replace=False)
+    rm_out = np.zeros((64, 2), np.int32)
+    for k, i in enumerate(idx):
+        m = np.zeros(1, np.int32)
+        o = np.zeros(1, np.int32)
+        lib.qbref_remove(rm.ctypes.data_as(qbo.i32p), rm.shape[0], S, LEVELS, pts[i].ctypes.data_as(qbo.f32p),
+                         m.ctypes.data_as(qbo.i32p), o.ctypes.data_as(qbo.i32p))
+        rm_out[k] = (m[0], o[0])
+    np.savez_compressed(os.path.join(HERE, "floor50k.npz"), n_points=50_000,
+                        nodes_sha256=np.frombuffer(hashlib.sha256(nodes.tobytes()).digest(), np.uint8),
+                        n_nodes=nodes.shape[0],
+                        paths_sha256=np.frombuffer(hashlib.sha256(nodes_path.tobytes()).digest(), np.uint8),
+                        points_sha256=np.frombuffer(hashlib.sha256(pts.tobytes()).digest(), np.uint8),
+                        remove_idx=idx.astype(np.int32), remove_out=rm_out,
+                        removed_sha256=np.frombuffer(hashlib.sha256(rm.tobytes()).digest(), np.uint8),
+                        ray_pos=pos, ray_dir=dirs, ref_model=model, ref_tlf=tlf)
+    print("floor50k:", nodes.shape[0], "nodes,", len(pos), "rays,", int((tlf[:, 3] >= 0).sum()), "leaf hits")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else qbo.REFERENCE_ROOT)
