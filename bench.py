@@ -192,6 +192,33 @@ def run_reference(args):
     return 0
 
 
+def measure_e2e(ctx, views, rays, world, flush, steps):
+    """Same views through the public C ABI into pinned host buffers: the
+    timed call includes the kernel and the copy of every frame to the host."""
+    import torch
+    import qubatron_gb300 as qb
+    host = [torch.empty((v.height_px, v.width_px, 4), dtype=torch.uint8, pin_memory=True) for v in views]
+    houts = []
+    for h in host:
+        o = qb.Outputs()
+        o.rgba8 = h.data_ptr()
+        houts.append(o)
+    for _ in range(2):
+        ctx.render_views(views, houts, on_device=False)
+    e2e_t = []
+    for _ in range(max(3, steps)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.render_views(views, houts, on_device=False)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = statistics.mean(e2e_t)
+    d2h = sum(h.numel() for h in host)
+    h2d = len(views) * 132  # qbc_view uniforms, passed as launch parameters
+    return {"value": world * rays / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "ms_per_step": 1000.0 * e2e_s}
+
+
 def run_gpu(args):
     import torch
     import qubatron_gb300 as qb
@@ -204,7 +231,11 @@ def run_gpu(args):
     w, scene, views, prep_s = prepare(WORKLOAD)
 
     ctx = qb.OctreeGLC(local)
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the library and the timing events must share it
+    # (torch's default stream is the legacy NULL stream, which the library
+    # does not take as a launch stream)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     ctx.upload_model(False, scene.colors, scene.normals)
     ctx.upload_octree(False, scene.nodes)
@@ -272,27 +303,12 @@ def run_gpu(args):
         ms = float(t.item())
     value = world * rays / (ms / 1000.0) / 1e6
 
-    # e2e through the public API with pinned host outputs
-    host = [torch.empty((v.height_px, v.width_px, 4), dtype=torch.uint8, pin_memory=True) for v in views]
-    houts = []
-    for h in host:
-        o = qb.Outputs()
-        o.rgba8 = h.data_ptr()
-        houts.append(o)
-    for _ in range(2):
-        ctx.render_views(views, houts, on_device=False)
-    e2e_t = []
-    for k in range(max(3, args.steps)):
-        flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        ctx.render_views(views, houts, on_device=False)
-        e2e_t.append(time.perf_counter() - t0)
-    e2e_s = statistics.mean(e2e_t)
-    d2h = sum(h.numel() for h in host)
-    h2d = len(views) * 132  # qbc_view uniforms, passed as launch parameters
+    e2e = None
+    if not args.no_e2e:
+        e2e = measure_e2e(ctx, views, rays, world, flush, args.steps)
 
     hbm, peak_kind = peaks()
+
     achieved = alg_bytes / (ms / 1000.0) / 1e9
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "render_kernel_traffic.json")
@@ -313,8 +329,7 @@ def run_gpu(args):
                          f"{scene.nodes.shape[0] * 36 / 1e9:.2f} GB > L2",
                    "parallelism": "replicas only" if world > 1 else "single GPU",
                    "prep_seconds": round(prep_s, 1)},
-        "e2e": {"value": world * rays / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+        "e2e": e2e,
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_kind": f"{peak_kind} (burst copy)",
@@ -341,6 +356,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", default=None)
     args = ap.parse_args()
     global WORKLOAD

@@ -257,7 +257,7 @@ __global__ void repack_nodes_kernel(const int4* __restrict__ raw, int64_t n, int
   }
 }
 
-// float3 points -> float4 texels (w = 1 for colour, as RGB32F reads; 0 for normals).
+// float3 points -> float4 texels; w = 1 as an RGB32F texel reads (colour and normal alike).
 __global__ void expand_attr_kernel(const float* __restrict__ raw, int64_t n, float4* __restrict__ out, float w) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     out[i] = make_float4(raw[3 * i], raw[3 * i + 1], raw[3 * i + 2], w);
@@ -506,7 +506,7 @@ extern "C" int qbc_upload(qbc_ctx* c, const void* data, int type, size_t size, s
       int64_t b = std::min(hi, a + chunk);
       QBC_CUDA(cudaMemcpyAsync(c->stage, base + a * 12, (size_t)(b - a) * 12, cudaMemcpyHostToDevice, c->stream));
       qbc::expand_attr_kernel<<<launch_grid(c, b - a), 256, 0, c->stream>>>((const float*)c->stage, b - a,
-                                                                             *arr + a, is_col ? 1.0f : 0.0f);
+                                                                             *arr + a, 1.0f);
       QBC_CUDA(cudaGetLastError());
       ++c->launches;
     }

@@ -39,7 +39,7 @@ struct DevTree {
 
 struct DevModel {
   const float4* col;  // (r, g, b, 1) per point, as an RGB32F texel reads
-  const float4* nrm;  // (x, y, z, 0)
+  const float4* nrm;  // (x, y, z, 1)
   int64_t n;
 };
 

@@ -64,6 +64,9 @@ SPECS = {
     "floor1m": SceneSpec(_lib.SCENE_FLOOR, 1_000_000, 1, 40, (50.0, 400.0), 20, (30.0, 200.0)),
     "room20m": SceneSpec(_lib.SCENE_ROOM, 20_000_000, 2, 200, (20.0, 300.0), 100, (10.0, 150.0), 0.05),
 }
+# the room scene at a quarter of the points: a profiling case whose node
+# arrays (~0.5 GB) still exceed L2 but keep an ncu capture short
+SPECS["room5m"] = SceneSpec(_lib.SCENE_ROOM, 5_000_000, 2, 200, (20.0, 300.0), 100, (10.0, 150.0), 0.05)
 
 
 @dataclass
@@ -173,6 +176,7 @@ class Workload:
 WORKLOADS = {
     "floor1m_640x480": Workload("floor1m_640x480", "floor1m", 640, 480, [FLOOR_POSE]),
     "room20m_1920x1080x16": Workload("room20m_1920x1080x16", "room20m", 1920, 1080, spline_poses(1002, 16)),
+    "room5m_1920x1080x1": Workload("room5m_1920x1080x1", "room5m", 1920, 1080, spline_poses(1002, 16)[:1]),
 }
 
 

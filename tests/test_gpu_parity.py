@@ -12,8 +12,10 @@ from helpers import bits, compare_frame, gpu_frame, oracle_scene, upload_scene
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module")
+@pytest.fixture
 def ctx():
+    """A fresh context per test: buffers uploaded by one test (a dynamic
+    tree, say) must not leak into the next."""
     import qubatron_gb300 as qb
     c = qb.OctreeGLC(0)
     yield c
