@@ -1,9 +1,8 @@
 // libqbcuda: context, uploads and the render kernel behind include/qbcuda.h.
 //
-// The render kernel is the per-pixel body of the reference's fragment shader
-// src/qubatron/shaders/octree_fsh.c:399-464 (ray generation, primary ray,
-// shadow ray, shading, light flare); the traversal is in trace.cuh. Build
-// flags: -fmad=false -prec-div=true -prec-sqrt=true -ftz=false.
+// The kernels are in render.cuh (per-pixel shader body, persistent) and
+// walker.cuh (the traversal). Build flags: -fmad=false -prec-div=true
+// -prec-sqrt=true -ftz=false.
 
 #include <cuda_runtime.h>
 
@@ -14,237 +13,11 @@
 
 #include "qbc_internal.h"
 #include "qbcuda.h"
-#include "trace.cuh"
+#include "render.cuh"
 
 using qbc::fail;
 
 namespace qbc {
-
-constexpr int kThreads = 128;      // 4 warps; each warp shades an 8x4 pixel tile
-constexpr int kTileW = 16;         // a block shades a 16x8 tile
-constexpr int kTileH = 8;
-constexpr int kMaxViewsPerLaunch = 32;
-
-struct ViewJob {
-  qbc_view v;
-  qbc_outputs o;  // device pointers
-  int32_t tiles_x;
-  int32_t tile_begin;
-  int32_t exact;  // cube recovery by inversion (see cube_shift_exact)
-  int32_t pad;
-};
-
-struct Batch {
-  ViewJob job[kMaxViewsPerLaunch];
-  int32_t n;
-  int32_t tiles_total;
-};
-
-// ---- main() helpers (octree_fsh.c:381-395 and GLSL built-ins) ----
-__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-
-__device__ __forceinline__ float3 normalize3(float3 v) {
-  float len = sqrtf(dot3(v, v));
-  return make_float3(v.x / len, v.y / len, v.z / len);
-}
-
-__device__ __forceinline__ float glsl_max(float x, float y) { return x < y ? y : x; }
-
-__device__ __forceinline__ float3 quat_rotate(const float* q, float3 v) {
-  // v + 2.0 * cross(q.xyz, cross(q.xyz, v) + q.w * v)
-  float c1x = q[1] * v.z - q[2] * v.y;
-  float c1y = q[2] * v.x - q[0] * v.z;
-  float c1z = q[0] * v.y - q[1] * v.x;
-  float ax = c1x + q[3] * v.x;
-  float ay = c1y + q[3] * v.y;
-  float az = c1z + q[3] * v.z;
-  float c2x = q[1] * az - q[2] * ay;
-  float c2y = q[2] * ax - q[0] * az;
-  float c2z = q[0] * ay - q[1] * ax;
-  return make_float3(v.x + 2.0f * c2x, v.y + 2.0f * c2y, v.z + 2.0f * c2z);
-}
-
-// GL float -> unorm8 for the RGBA8 colour target.
-__device__ __forceinline__ uint32_t unorm8(float f) {
-  if (!(f > 0.0f)) return 0u;
-  if (f >= 1.0f) return 255u;
-  return (uint32_t)(f * 255.0f + 0.5f);
-}
-
-template <bool EXACT>
-__device__ __forceinline__ void shade_pixel(const DevScene& sc, const ViewJob& J, int i, int j, const Stack& st) {
-  const qbc_view& v = J.v;
-  const float4 bc = make_float4(v.basecube[0], v.basecube[1], v.basecube[2], v.basecube[3]);
-  const float3 camfp = make_float3(v.camfp[0], v.camfp[1], v.camfp[2]);
-  const float3 light = make_float3(v.light[0], v.light[1], v.light[2]);
-  uint32_t f = 0;
-  int32_t leaf[4] = {-1, -1, -1, -1};
-  uint32_t vis[4] = {0, 0, 0, 0};
-  float4 ispo = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  float4 col = ispo;
-  bool written = true;
-
-  // ray generation (octree_fsh.c:402-413); coord is the pixel centre
-  float cx = ((float)i + 0.5f) * v.coord_scale[0];
-  float cy = ((float)j + 0.5f) * v.coord_scale[1];
-  float3 csv = make_float3(cx - v.cfp[0], cy - v.cfp[1], 0.0f - v.cfp[2]);
-  csv = quat_rotate(v.qz, csv);
-  csv = quat_rotate(v.qx, csv);
-
-  float3 ncsv = normalize3(csv);
-  float cosang = dot3(make_float3(v.ncamlight[0], v.ncamlight[1], v.ncamlight[2]), ncsv);
-  bool flare = cosang > v.flare_cos && cosang <= 1.0f;
-
-  TraceOut res;
-  trace<EXACT>(sc, bc, v.maxlevel, camfp, csv, st, res);
-  vis[0] = res.vis_s;
-  vis[1] = res.vis_d;
-  if (res.oob) f |= QBC_PX_OOB;
-  if (res.status == kDiscard) {
-    f |= QBC_PX_DISCARD;
-    written = false;
-  } else {
-    if (res.status == kLeaf) {
-      f |= QBC_PX_PRIMARY_LEAF;
-      leaf[0] = res.leaf_s;
-      leaf[1] = res.leaf_d;
-    }
-    ispo = res.isp;
-    col = res.col;
-
-    if (res.isp.w > 0.0f) {
-      // shadow ray and shading (octree_fsh.c:431-449)
-      f |= QBC_PX_SHADED;
-      float3 lghtv = make_float3(res.isp.x - light.x, res.isp.y - light.y, res.isp.z - light.z);
-      TraceOut lc;
-      trace<EXACT>(sc, bc, v.maxlevel, light, lghtv, st, lc);
-      vis[2] = lc.vis_s;
-      vis[3] = lc.vis_d;
-      if (lc.oob) f |= QBC_PX_OOB;
-      if (lc.status == kDiscard) {
-        f |= QBC_PX_DISCARD;
-        written = false;
-      } else {
-        if (lc.status == kLeaf) {
-          f |= QBC_PX_SHADOW_LEAF;
-          leaf[2] = lc.leaf_s;
-          leaf[3] = lc.leaf_d;
-        }
-        float ix = lc.isp.x - res.isp.x, iy = lc.isp.y - res.isp.y, iz = lc.isp.z - res.isp.z;
-        float sqr = ix * ix + iy * iy + iz * iz;
-        float3 nl = normalize3(make_float3(-lghtv.x, -lghtv.y, -lghtv.z));
-        float3 nn = normalize3(make_float3(res.nrm.x, res.nrm.y, res.nrm.z));
-        float3 nc = normalize3(make_float3(-csv.x, -csv.y, -csv.z));
-        float lght_nrm_ang = glsl_max(dot3(nl, nn), 0.0f);
-        float camv_nrm_ang = glsl_max(dot3(nc, nn), 0.0f);
-        float lit = (15.0f < sqr) ? 0.0f : 1.0f;  // step(sqr, 15.0)
-        if (lit != 0.0f) f |= QBC_PX_LIT;
-        float k = 0.1f + 0.2f * camv_nrm_ang + lght_nrm_ang * lit * 0.7f;
-        col.x = col.x * k;
-        col.y = col.y * k;
-        col.z = col.z * k;
-        col.z *= 0.7f;
-        float g = (float)v.shoot * camv_nrm_ang * 0.1f;
-        col.x += g;
-        col.y += g;
-        col.z += g;
-      }
-    }
-
-    if (written && flare) {
-      // light flare (octree_fsh.c:452-459)
-      f |= QBC_PX_FLARE_TEST;
-      float3 lghtv = make_float3(light.x - camfp.x, light.y - camfp.y, light.z - camfp.z);
-      TraceOut lc;
-      trace<EXACT>(sc, bc, v.maxlevel, camfp, lghtv, st, lc);
-      if (lc.oob) f |= QBC_PX_OOB;
-      if (lc.status == kDiscard) {
-        f |= QBC_PX_DISCARD;
-        written = false;
-      } else {
-        float resv_x = lc.isp.x - camfp.x;
-        if (resv_x / lghtv.x > 1.0f) {
-          f |= QBC_PX_FLARE_WHITE;
-          col = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-        }
-      }
-    }
-  }
-  if (!written) col = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-
-  const int64_t o = (int64_t)j * v.width_px + i;
-  const qbc_outputs& out = J.o;
-  if (out.rgba8)
-    reinterpret_cast<uint32_t*>(out.rgba8)[o] =
-        unorm8(col.x) | (unorm8(col.y) << 8) | (unorm8(col.z) << 16) | (unorm8(col.w) << 24);
-  if (out.rgba32f) reinterpret_cast<float4*>(out.rgba32f)[o] = col;
-  if (out.flags) out.flags[o] = f;
-  if (out.leaf) reinterpret_cast<int4*>(out.leaf)[o] = make_int4(leaf[0], leaf[1], leaf[2], leaf[3]);
-  if (out.isp) reinterpret_cast<float4*>(out.isp)[o] = ispo;
-  if (out.visits) reinterpret_cast<uint4*>(out.visits)[o] = make_uint4(vis[0], vis[1], vis[2], vis[3]);
-}
-
-__global__ void __launch_bounds__(kThreads) render_kernel(DevScene sc, const __grid_constant__ Batch batch) {
-  extern __shared__ uint32_t smem[];
-  const int tile = blockIdx.x;
-  // the view owning this tile: last job with tile_begin <= tile
-  int lo = 0, hi = batch.n - 1;
-  while (lo < hi) {
-    int mid = (lo + hi + 1) >> 1;
-    if (batch.job[mid].tile_begin <= tile)
-      lo = mid;
-    else
-      hi = mid - 1;
-  }
-  const ViewJob& J = batch.job[lo];
-  const int t = tile - J.tile_begin;
-  const int tx = t % J.tiles_x, ty = t / J.tiles_x;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int px = tx * kTileW + (warp & 1) * 8 + (lane & 7);
-  const int py = ty * kTileH + (warp >> 1) * 4 + (lane >> 3);
-  if (px >= J.v.width_px || py >= J.v.height_px) return;
-  Stack st{smem + threadIdx.x, kThreads};
-  if (J.exact)
-    shade_pixel<true>(sc, J, px, py, st);
-  else
-    shade_pixel<false>(sc, J, px, py, st);
-}
-
-struct RayJob {
-  const float* pos;
-  const float* dir;
-  int64_t n;
-  float4 bc;
-  int32_t maxlevel;
-  int32_t exact;
-  qbc_ray_hits o;
-};
-
-template <bool EXACT>
-__device__ __forceinline__ void ray_query(const DevScene& sc, const RayJob& J, int64_t i, const Stack& st) {
-  float3 p = make_float3(J.pos[3 * i], J.pos[3 * i + 1], J.pos[3 * i + 2]);
-  float3 d = make_float3(J.dir[3 * i], J.dir[3 * i + 1], J.dir[3 * i + 2]);
-  TraceOut r;
-  trace<EXACT>(sc, J.bc, J.maxlevel, p, d, st, r);
-  if (J.o.status) J.o.status[i] = r.status;
-  if (J.o.leaf) reinterpret_cast<int2*>(J.o.leaf)[i] = make_int2(r.leaf_s, r.leaf_d);
-  if (J.o.model) reinterpret_cast<int2*>(J.o.model)[i] = make_int2(r.model_s, r.model_d);
-  if (J.o.isp) reinterpret_cast<float4*>(J.o.isp)[i] = r.isp;
-  if (J.o.col) reinterpret_cast<float4*>(J.o.col)[i] = r.col;
-  if (J.o.nrm) reinterpret_cast<float4*>(J.o.nrm)[i] = r.nrm;
-  if (J.o.visits) reinterpret_cast<uint2*>(J.o.visits)[i] = make_uint2(r.vis_s, r.vis_d);
-}
-
-__global__ void __launch_bounds__(kThreads) rays_kernel(DevScene sc, const __grid_constant__ RayJob job) {
-  extern __shared__ uint32_t smem[];
-  const int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x;
-  if (i >= job.n) return;
-  Stack st{smem + threadIdx.x, kThreads};
-  if (job.exact)
-    ray_query<true>(sc, job, i, st);
-  else
-    ray_query<false>(sc, job, i, st);
-}
 
 // Split 12-int nodes (octree.c:11-14) into 32-byte child blocks + model index.
 __global__ void repack_nodes_kernel(const int4* __restrict__ raw, int64_t n, int4* __restrict__ child,
@@ -294,6 +67,9 @@ struct qbc_ctx {
   size_t stage_bytes = 0;
   void* scratch = nullptr;  // device outputs for host-output renders
   size_t scratch_bytes = 0;
+  unsigned int* queue = nullptr;  // global tile counter of the persistent render kernel
+  int render_blocks[4] = {0, 0, 0, 0};  // resident blocks per SM of each render_kernel variant
+  int attr_done = 0;
   int64_t launches = 0;
 };
 
@@ -374,6 +150,12 @@ extern "C" int qbc_create(int device, qbc_ctx** out) {
     delete c;
     return cuda_fail(e, "qbc_create");
   }
+  if (e == cudaSuccess) e = cudaMalloc(&c->queue, sizeof(unsigned int));
+  if (e != cudaSuccess) {
+    if (c->own) cudaStreamDestroy(c->own);
+    delete c;
+    return cuda_fail(e, "qbc_create");
+  }
   c->stream = c->own;
   *out = c;
   return QBC_OK;
@@ -391,6 +173,7 @@ extern "C" int qbc_destroy(qbc_ctx* c) {
   }
   cudaFree(c->stage);
   cudaFree(c->scratch);
+  cudaFree(c->queue);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return QBC_OK;
@@ -543,34 +326,56 @@ void** out_slot(qbc_outputs& o, int k) {
   }
 }
 
+template <bool EXACT, bool DYN>
+int launch_render(qbc_ctx* c, const qbc::Batch& b, size_t smem) {
+  auto kern = qbc::render_kernel<EXACT, DYN>;
+  const int variant = (EXACT ? 1 : 0) + (DYN ? 2 : 0);
+  if (!(c->attr_done & (1 << variant))) {
+    QBC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+    c->attr_done |= 1 << variant;
+  }
+  int per_sm = 0;
+  QBC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, qbc::kThreads, smem));
+  if (per_sm < 1) return fail(QBC_E_STATE, "render_kernel: no block fits on an SM with %zu B shared memory", smem);
+  c->render_blocks[variant] = per_sm;
+  // persistent: one wave of resident blocks, never more blocks than warp tiles
+  int64_t blocks = std::min<int64_t>((int64_t)per_sm * c->sm_count, ((int64_t)b.tiles_total + 3) / 4);
+  blocks = std::max<int64_t>(blocks, 1);
+  QBC_CUDA(cudaMemsetAsync(c->queue, 0, sizeof(unsigned int), c->stream));
+  kern<<<(unsigned)blocks, qbc::kThreads, smem, c->stream>>>(device_scene(c), b, c->queue);
+  QBC_CUDA(cudaGetLastError());
+  ++c->launches;
+  return QBC_OK;
+}
+
 int launch_batch(qbc_ctx* c, const qbc_view* views, const qbc_outputs* dev_outs, int n) {
   qbc::Batch* b = new qbc::Batch();
   int tiles = 0, maxlevel = 0;
+  bool exact = true;
   for (int i = 0; i < n; ++i) {
     qbc::ViewJob& J = b->job[i];
     J.v = views[i];
     J.o = dev_outs[i];
-    J.tiles_x = (views[i].width_px + qbc::kTileW - 1) / qbc::kTileW;
-    int tiles_y = (views[i].height_px + qbc::kTileH - 1) / qbc::kTileH;
+    J.tiles_x = (views[i].width_px + 7) / 8;
+    int tiles_y = (views[i].height_px + 3) / 4;
     J.tile_begin = tiles;
-    J.exact = qbc::cube_shift_exact(views[i]) ? 1 : 0;
     tiles += J.tiles_x * tiles_y;
     maxlevel = std::max(maxlevel, views[i].maxlevel);
+    exact = exact && qbc::cube_shift_exact(views[i]);
   }
   b->n = n;
   b->tiles_total = tiles;
-  size_t smem = (size_t)maxlevel * 3 * qbc::kThreads * sizeof(uint32_t);
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(qbc::render_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024);
-    attr_set = true;
-  }
-  qbc::render_kernel<<<tiles, qbc::kThreads, smem, c->stream>>>(device_scene(c), *b);
+  b->max_level = maxlevel;
+  const bool dyn = c->tree[1].n > 0;
+  const size_t words = (size_t)(dyn ? 3 : 2) * maxlevel + qbc::kPixWords;
+  const size_t smem = words * qbc::kThreads * sizeof(uint32_t);
+  int rc;
+  if (exact)
+    rc = dyn ? launch_render<true, true>(c, *b, smem) : launch_render<true, false>(c, *b, smem);
+  else
+    rc = dyn ? launch_render<false, true>(c, *b, smem) : launch_render<false, false>(c, *b, smem);
   delete b;
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_fail(e, "render_kernel launch");
-  ++c->launches;
-  return QBC_OK;
+  return rc;
 }
 
 }  // namespace
@@ -656,7 +461,6 @@ extern "C" int qbc_trace_rays(qbc_ctx* c, const float* pos, const float* dir, in
   job.n = n;
   job.bc = make_float4(basecube[0], basecube[1], basecube[2], basecube[3]);
   job.maxlevel = maxlevel;
-  job.exact = qbc::cube_shift_exact(probe) ? 1 : 0;
   // per-ray bytes of each output, in qbc_ray_hits order
   const size_t bytes[7] = {4, 8, 8, 16, 16, 16, 8};
   void* const* hs[7] = {(void* const*)&out->status, (void* const*)&out->leaf, (void* const*)&out->model,
@@ -702,10 +506,19 @@ extern "C" int qbc_trace_rays(qbc_ctx* c, const float* pos, const float* dir, in
   job.o.col = (float*)dv[4];
   job.o.nrm = (float*)dv[5];
   job.o.visits = (uint32_t*)dv[6];
-  size_t smem = (size_t)maxlevel * 3 * qbc::kThreads * sizeof(uint32_t);
+  const bool dyn = c->tree[1].n > 0;
+  size_t smem = (size_t)maxlevel * (dyn ? 3 : 2) * qbc::kThreads * sizeof(uint32_t);
   int64_t blocks = (n + qbc::kThreads - 1) / qbc::kThreads;
   if (blocks > INT32_MAX) return fail(QBC_E_ARG, "qbc_trace_rays: too many rays");
-  qbc::rays_kernel<<<(unsigned)blocks, qbc::kThreads, smem, c->stream>>>(device_scene(c), job);
+  const bool exact = qbc::cube_shift_exact(probe);
+  if (exact && dyn)
+    qbc::rays_kernel<true, true><<<(unsigned)blocks, qbc::kThreads, smem, c->stream>>>(device_scene(c), job);
+  else if (exact)
+    qbc::rays_kernel<true, false><<<(unsigned)blocks, qbc::kThreads, smem, c->stream>>>(device_scene(c), job);
+  else if (dyn)
+    qbc::rays_kernel<false, true><<<(unsigned)blocks, qbc::kThreads, smem, c->stream>>>(device_scene(c), job);
+  else
+    qbc::rays_kernel<false, false><<<(unsigned)blocks, qbc::kThreads, smem, c->stream>>>(device_scene(c), job);
   QBC_CUDA(cudaGetLastError());
   ++c->launches;
   if (!on_device) {

@@ -1,0 +1,408 @@
+// Render and ray-query kernels on the resumable walker (walker.cuh).
+//
+// render_kernel is the per-pixel body of the reference's fragment shader
+// (src/qubatron/shaders/octree_fsh.c:399-464): ray generation, primary ray,
+// shadow ray from the light, shading, light flare. It is persistent: every
+// warp takes 8x4 pixel tiles from a global queue, and a lane whose ray ended
+// continues at once with the next ray of its pixel (shadow, flare) or with
+// the next pixel of its warp's tile, so lanes do not idle behind the
+// slowest ray of the warp.
+#pragma once
+
+#include "qbcuda.h"
+#include "walker.cuh"
+
+namespace qbc {
+
+constexpr int kThreads = 128;  // 4 warps
+constexpr int kMaxViewsPerLaunch = 32;
+constexpr int kPixWords = 26;  // per-lane pixel state words in shared memory
+
+struct ViewJob {
+  qbc_view v;
+  qbc_outputs o;  // device pointers
+  int32_t tiles_x;     // 8-pixel-wide warp tiles per row
+  int32_t tile_begin;  // first global tile index of this view
+  int32_t pad[2];
+};
+
+struct Batch {
+  ViewJob job[kMaxViewsPerLaunch];
+  int32_t n;
+  int32_t tiles_total;
+  int32_t max_level;  // largest maxlevel of the batch: stack depth
+  int32_t pad;
+};
+
+// ---- main() helpers (octree_fsh.c:381-395 and GLSL built-ins) ----
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+__device__ __forceinline__ float3 normalize3(float3 v) {
+  float len = sqrtf(dot3(v, v));
+  return make_float3(v.x / len, v.y / len, v.z / len);
+}
+
+__device__ __forceinline__ float glsl_max(float x, float y) { return x < y ? y : x; }
+
+__device__ __forceinline__ float3 quat_rotate(const float* q, float3 v) {
+  // v + 2.0 * cross(q.xyz, cross(q.xyz, v) + q.w * v)
+  float c1x = q[1] * v.z - q[2] * v.y;
+  float c1y = q[2] * v.x - q[0] * v.z;
+  float c1z = q[0] * v.y - q[1] * v.x;
+  float ax = c1x + q[3] * v.x;
+  float ay = c1y + q[3] * v.y;
+  float az = c1z + q[3] * v.z;
+  float c2x = q[1] * az - q[2] * ay;
+  float c2y = q[2] * ax - q[0] * az;
+  float c2z = q[0] * ay - q[1] * ax;
+  return make_float3(v.x + 2.0f * c2x, v.y + 2.0f * c2y, v.z + 2.0f * c2z);
+}
+
+// GL float -> unorm8 for the RGBA8 colour target.
+__device__ __forceinline__ uint32_t unorm8(float f) {
+  if (!(f > 0.0f)) return 0u;
+  if (f >= 1.0f) return 255u;
+  return (uint32_t)(f * 255.0f + 0.5f);
+}
+
+__device__ __forceinline__ float4 view_bc(const qbc_view& v) {
+  return make_float4(v.basecube[0], v.basecube[1], v.basecube[2], v.basecube[3]);
+}
+
+// Per-lane pixel state in shared memory, word k at px[k * kThreads].
+enum PixWord : int {
+  kPxView = 0, kPxXY, kPxFlags,
+  kPxCsv,                  // 3 words: camera ray direction
+  kPxIsp = kPxCsv + 3,     // 4 words: primary intersection
+  kPxCol = kPxIsp + 4,     // 4 words: colour (primary texel, then shaded)
+  kPxNrm = kPxCol + 4,     // 3 words: primary normal
+  kPxLeaf = kPxNrm + 3,    // 4 words: primary leaf s, d; shadow leaf s, d
+  kPxVis = kPxLeaf + 4,    // 4 words: visits primary s, d; shadow s, d
+  kPxEnd = kPxVis + 4
+};
+static_assert(kPxEnd <= kPixWords, "pixel state");
+
+enum Phase : int { kIdle = 0, kPrimary = 1, kShadow = 2, kFlare = 3 };
+
+// Internal flag: the pixel's camera ray is within the flare angle. The public
+// QBC_PX_FLARE_TEST is set only when the flare ray is actually traced.
+constexpr uint32_t kWantFlare = 1u << 31;
+
+struct PixRef {
+  uint32_t* base;
+  __device__ __forceinline__ uint32_t& w(int k) const { return base[k * kThreads]; }
+  __device__ __forceinline__ float& f(int k) const { return reinterpret_cast<float&>(base[k * kThreads]); }
+};
+
+template <bool EXACT, bool DYN>
+struct Shader {
+  const DevScene& sc;
+  const Batch& batch;
+  Stack st;
+  PixRef px;
+  Walker<EXACT, DYN> w;
+  int phase;     // kind of the lane's current ray, kIdle without a pixel
+  bool running;  // the ray is being walked
+  int result;    // status of the ray once it ended
+  int maxlevel;
+  float4 bc;
+
+  __device__ __forceinline__ const qbc_view& view() const { return batch.job[px.w(kPxView)].v; }
+
+  __device__ __forceinline__ void write_out(float4 col) {
+    const ViewJob& J = batch.job[px.w(kPxView)];
+    uint32_t xy = px.w(kPxXY);
+    int i = (int)(xy & 0xFFFFu), j = (int)(xy >> 16);
+    const int64_t o = (int64_t)j * J.v.width_px + i;
+    const qbc_outputs& out = J.o;
+    if (out.rgba8)
+      reinterpret_cast<uint32_t*>(out.rgba8)[o] =
+          unorm8(col.x) | (unorm8(col.y) << 8) | (unorm8(col.z) << 16) | (unorm8(col.w) << 24);
+    if (out.rgba32f) reinterpret_cast<float4*>(out.rgba32f)[o] = col;
+    if (out.flags) out.flags[o] = px.w(kPxFlags) & ~kWantFlare;
+    if (out.leaf)
+      reinterpret_cast<int4*>(out.leaf)[o] = make_int4((int32_t)px.w(kPxLeaf), (int32_t)px.w(kPxLeaf + 1),
+                                                       (int32_t)px.w(kPxLeaf + 2), (int32_t)px.w(kPxLeaf + 3));
+    if (out.isp)
+      reinterpret_cast<float4*>(out.isp)[o] =
+          make_float4(px.f(kPxIsp), px.f(kPxIsp + 1), px.f(kPxIsp + 2), px.f(kPxIsp + 3));
+    if (out.visits)
+      reinterpret_cast<uint4*>(out.visits)[o] =
+          make_uint4(px.w(kPxVis), px.w(kPxVis + 1), px.w(kPxVis + 2), px.w(kPxVis + 3));
+    phase = kIdle;
+  }
+
+  __device__ __forceinline__ void discard() {
+    px.w(kPxFlags) |= QBC_PX_DISCARD;
+    write_out(make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+  }
+
+  // Pixel (i, j) of view vi: ray generation (octree_fsh.c:402-418). Sets the
+  // primary ray into (rp, rd).
+  __device__ __forceinline__ void begin_pixel(int vi, int i, int j, float3& rp, float3& rd) {
+    px.w(kPxView) = (uint32_t)vi;
+    px.w(kPxXY) = (uint32_t)i | ((uint32_t)j << 16);
+    const qbc_view& v = batch.job[vi].v;
+    maxlevel = v.maxlevel;
+    bc = view_bc(v);
+    float cx = ((float)i + 0.5f) * v.coord_scale[0];
+    float cy = ((float)j + 0.5f) * v.coord_scale[1];
+    float3 csv = make_float3(cx - v.cfp[0], cy - v.cfp[1], 0.0f - v.cfp[2]);
+    csv = quat_rotate(v.qz, csv);
+    csv = quat_rotate(v.qx, csv);
+    float3 ncsv = normalize3(csv);
+    float cosang = dot3(make_float3(v.ncamlight[0], v.ncamlight[1], v.ncamlight[2]), ncsv);
+    px.w(kPxFlags) = (cosang > v.flare_cos && cosang <= 1.0f) ? kWantFlare : 0u;
+    px.f(kPxCsv) = csv.x;
+    px.f(kPxCsv + 1) = csv.y;
+    px.f(kPxCsv + 2) = csv.z;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      px.w(kPxLeaf + k) = (uint32_t)-1;
+      px.w(kPxVis + k) = 0u;
+      px.f(kPxIsp + k) = 0.0f;
+    }
+    phase = kPrimary;
+    rp = make_float3(v.camfp[0], v.camfp[1], v.camfp[2]);
+    rd = csv;
+  }
+
+  // Flare ray (octree_fsh.c:452-459) if the pixel wants one: returns true and
+  // sets (rp, rd); otherwise writes the pixel.
+  __device__ __forceinline__ bool flare_or_finish(float4 col, float3& rp, float3& rd) {
+    if (px.w(kPxFlags) & kWantFlare) {
+      px.w(kPxFlags) |= QBC_PX_FLARE_TEST;
+      const qbc_view& v = view();
+#pragma unroll
+      for (int k = 0; k < 4; ++k) px.f(kPxCol + k) = (&col.x)[k];
+      rp = make_float3(v.camfp[0], v.camfp[1], v.camfp[2]);
+      rd = make_float3(v.light[0] - rp.x, v.light[1] - rp.y, v.light[2] - rp.z);
+      phase = kFlare;
+      return true;
+    }
+    write_out(col);
+    return false;
+  }
+
+  // The lane's ray ended with `result`: record it and decide the pixel's next
+  // ray. Returns true with (rp, rd) set when another ray of this pixel starts.
+  __device__ __forceinline__ bool consume(float3& rp, float3& rd) {
+    const int r = result;
+    float4 col = make_float4(0.f, 0.f, 0.f, 0.f), nrm = col, isp = col;
+    if (r == kLeaf) {
+      int32_t ms, md;
+      w.leaf(sc, ms, md, col, nrm);
+      isp = w.e;
+    }
+    if (w.oob) px.w(kPxFlags) |= QBC_PX_OOB;
+
+    if (phase == kPrimary) {
+      px.w(kPxVis) = w.vis_s;
+      px.w(kPxVis + 1) = w.vis_d;
+      if (r == kLeaf) {
+        px.w(kPxFlags) |= QBC_PX_PRIMARY_LEAF;
+        px.w(kPxLeaf) = (uint32_t)w.ns;
+        px.w(kPxLeaf + 1) = (uint32_t)w.nd;
+      }
+      px.f(kPxIsp) = isp.x;
+      px.f(kPxIsp + 1) = isp.y;
+      px.f(kPxIsp + 2) = isp.z;
+      px.f(kPxIsp + 3) = isp.w;
+      if (isp.w > 0.0f) {
+        // shadow ray from the light to the hit (octree_fsh.c:431-432)
+        px.w(kPxFlags) |= QBC_PX_SHADED;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) px.f(kPxCol + k) = (&col.x)[k];
+        px.f(kPxNrm) = nrm.x;
+        px.f(kPxNrm + 1) = nrm.y;
+        px.f(kPxNrm + 2) = nrm.z;
+        const qbc_view& v = view();
+        rp = make_float3(v.light[0], v.light[1], v.light[2]);
+        rd = make_float3(isp.x - rp.x, isp.y - rp.y, isp.z - rp.z);
+        phase = kShadow;
+        return true;
+      }
+      return flare_or_finish(col, rp, rd);
+    }
+    if (phase == kShadow) {
+      // shading (octree_fsh.c:433-449)
+      px.w(kPxVis + 2) = w.vis_s;
+      px.w(kPxVis + 3) = w.vis_d;
+      if (r == kLeaf) {
+        px.w(kPxFlags) |= QBC_PX_SHADOW_LEAF;
+        px.w(kPxLeaf + 2) = (uint32_t)w.ns;
+        px.w(kPxLeaf + 3) = (uint32_t)w.nd;
+      }
+      const qbc_view& v = view();
+      float4 pi = make_float4(px.f(kPxIsp), px.f(kPxIsp + 1), px.f(kPxIsp + 2), px.f(kPxIsp + 3));
+      float4 pc = make_float4(px.f(kPxCol), px.f(kPxCol + 1), px.f(kPxCol + 2), px.f(kPxCol + 3));
+      float3 pn = make_float3(px.f(kPxNrm), px.f(kPxNrm + 1), px.f(kPxNrm + 2));
+      float3 csv = make_float3(px.f(kPxCsv), px.f(kPxCsv + 1), px.f(kPxCsv + 2));
+      float3 lghtv = make_float3(pi.x - v.light[0], pi.y - v.light[1], pi.z - v.light[2]);
+      float ix = isp.x - pi.x, iy = isp.y - pi.y, iz = isp.z - pi.z;
+      float sqr = ix * ix + iy * iy + iz * iz;
+      float3 nl = normalize3(make_float3(-lghtv.x, -lghtv.y, -lghtv.z));
+      float3 nn = normalize3(pn);
+      float3 nc = normalize3(make_float3(-csv.x, -csv.y, -csv.z));
+      float lght_nrm_ang = glsl_max(dot3(nl, nn), 0.0f);
+      float camv_nrm_ang = glsl_max(dot3(nc, nn), 0.0f);
+      float lit = (15.0f < sqr) ? 0.0f : 1.0f;  // step(sqr, 15.0)
+      if (lit != 0.0f) px.w(kPxFlags) |= QBC_PX_LIT;
+      float k = 0.1f + 0.2f * camv_nrm_ang + lght_nrm_ang * lit * 0.7f;
+      pc.x = pc.x * k;
+      pc.y = pc.y * k;
+      pc.z = pc.z * k;
+      pc.z *= 0.7f;
+      float g = (float)v.shoot * camv_nrm_ang * 0.1f;
+      pc.x += g;
+      pc.y += g;
+      pc.z += g;
+      return flare_or_finish(pc, rp, rd);
+    }
+    // flare ray ended (octree_fsh.c:456-458)
+    const qbc_view& v = view();
+    float4 pc = make_float4(px.f(kPxCol), px.f(kPxCol + 1), px.f(kPxCol + 2), px.f(kPxCol + 3));
+    float resv_x = isp.x - v.camfp[0];
+    float lx = v.light[0] - v.camfp[0];
+    if (resv_x / lx > 1.0f) {
+      px.w(kPxFlags) |= QBC_PX_FLARE_WHITE;
+      pc = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+    }
+    write_out(pc);
+    return false;
+  }
+};
+
+// Global tile queue: tiles are 8x4 pixel warp tiles, numbered view by view.
+__device__ __forceinline__ int tile_view(const Batch& b, int tile) {
+  int lo = 0, hi = b.n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (b.job[mid].tile_begin <= tile)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// Lanes whose ray ended wait until at least this many lanes of the warp need
+// service (or no ray is left running); then ray transitions, refills and ray
+// starts run for all of them together instead of one lane at a time.
+constexpr int kServiceMin = 8;
+
+template <bool EXACT, bool DYN>
+__global__ void __launch_bounds__(kThreads) render_kernel(DevScene sc, const __grid_constant__ Batch batch,
+                                                          unsigned int* queue) {
+  extern __shared__ uint32_t smem[];
+  const int tid = threadIdx.x, lane = tid & 31;
+  constexpr int kW = Walker<EXACT, DYN>::kWords;
+  Shader<EXACT, DYN> S{sc, batch, Stack{smem + tid, kThreads}, PixRef{smem + kW * batch.max_level * kThreads + tid}};
+  S.phase = kIdle;
+  S.running = false;
+  S.result = 0;
+  S.maxlevel = 0;
+  S.bc = make_float4(0.f, 0.f, 0.f, 0.f);
+  int tile = 0, consumed = 32;  // warp-uniform
+  bool exhausted = false;
+  const unsigned lt_mask = (1u << lane) - 1u;
+
+  for (;;) {
+    const unsigned run = __ballot_sync(0xFFFFFFFFu, S.running);
+    const int waiting = 32 - __popc(run);
+    if (run == 0 || waiting >= kServiceMin) {
+      // ---- service: consume ended rays, refill, start new rays together ----
+      float3 rp = make_float3(0.f, 0.f, 0.f), rd = rp;
+      bool go = false;
+      if (!S.running && S.phase != kIdle) go = S.consume(rp, rd);
+      unsigned idle = __ballot_sync(0xFFFFFFFFu, S.phase == kIdle);
+      while (idle && !exhausted) {
+        if (consumed >= 32) {
+          unsigned t0 = 0;
+          if (lane == 0) t0 = atomicAdd(queue, 1u);
+          tile = (int)__shfl_sync(0xFFFFFFFFu, t0, 0);
+          consumed = 0;
+          if (tile >= batch.tiles_total) {
+            exhausted = true;
+            break;
+          }
+        }
+        const int avail = 32 - consumed;
+        const int rank = __popc(idle & lt_mask);
+        if (((idle >> lane) & 1u) && rank < avail) {
+          const int slot = consumed + rank;
+          const int vi = tile_view(batch, tile);
+          const ViewJob& J = batch.job[vi];
+          const int t = tile - J.tile_begin;
+          const int x = (t % J.tiles_x) * 8 + (slot & 7);
+          const int y = (t / J.tiles_x) * 4 + (slot >> 3);
+          if (x < J.v.width_px && y < J.v.height_px) {
+            S.begin_pixel(vi, x, y, rp, rd);
+            go = true;
+          }
+        }
+        consumed += min(avail, __popc(idle));
+        idle = __ballot_sync(0xFFFFFFFFu, S.phase == kIdle);
+      }
+      if (go) {
+        if (S.w.start(S.bc, rp, rd) == kDiscard)
+          S.discard();
+        else
+          S.running = true;
+      }
+      if (exhausted && __ballot_sync(0xFFFFFFFFu, S.phase != kIdle) == 0) break;
+    }
+    if (S.running) {
+      const int r = S.w.step(sc, S.maxlevel, S.bc, S.st);
+      if (r != kRunning) {
+        S.running = false;
+        S.result = r;
+      }
+    }
+  }
+}
+
+struct RayJob {
+  const float* pos;
+  const float* dir;
+  int64_t n;
+  float4 bc;
+  int32_t maxlevel;
+  int32_t pad;
+  qbc_ray_hits o;
+};
+
+template <bool EXACT, bool DYN>
+__global__ void __launch_bounds__(kThreads) rays_kernel(DevScene sc, const __grid_constant__ RayJob job) {
+  extern __shared__ uint32_t smem[];
+  const int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x;
+  if (i >= job.n) return;
+  Stack st{smem + threadIdx.x, kThreads};
+  Walker<EXACT, DYN> w;
+  float3 p = make_float3(job.pos[3 * i], job.pos[3 * i + 1], job.pos[3 * i + 2]);
+  float3 d = make_float3(job.dir[3 * i], job.dir[3 * i + 1], job.dir[3 * i + 2]);
+  int r = w.start(job.bc, p, d);
+  if (r != kDiscard) {
+    do {
+      r = w.step(sc, job.maxlevel, job.bc, st);
+    } while (r == kRunning);
+  }
+  int32_t ms = -1, md = -1, ls = -1, ld = -1;
+  float4 col = make_float4(0.f, 0.f, 0.f, 0.f), nrm = col, isp = col;
+  if (r == kLeaf) {
+    w.leaf(sc, ms, md, col, nrm);
+    isp = w.e;
+    ls = w.ns;
+    ld = w.nd;
+  }
+  const qbc_ray_hits& o = job.o;
+  if (o.status) o.status[i] = r == kDiscard ? kDiscard : (r == kLeaf ? kLeaf : kMiss);
+  if (o.leaf) reinterpret_cast<int2*>(o.leaf)[i] = make_int2(ls, ld);
+  if (o.model) reinterpret_cast<int2*>(o.model)[i] = make_int2(ms, md);
+  if (o.isp) reinterpret_cast<float4*>(o.isp)[i] = isp;
+  if (o.col) reinterpret_cast<float4*>(o.col)[i] = col;
+  if (o.nrm) reinterpret_cast<float4*>(o.nrm)[i] = nrm;
+  if (o.visits) reinterpret_cast<uint2*>(o.visits)[i] = r == kDiscard ? make_uint2(0, 0) : make_uint2(w.vis_s, w.vis_d);
+}
+
+}  // namespace qbc

@@ -1,0 +1,271 @@
+// Resumable traversal of qubatron's sparse octree, one step per call.
+//
+// Walks the static and dynamic trees together exactly as `cube_trace_line`
+// of src/qubatron/shaders/octree_fsh.c:138-379 does, but as a state machine:
+// start() does the basecube entry; each step() does one subnode test and one
+// descent (after popping as far as needed). A persistent kernel can then give
+// a lane whose ray ended a new ray, instead of idling until the slowest ray
+// of its warp ends.
+//
+// Same arithmetic contract as trace.cuh (FP32 in the shader's order,
+// -fmad=false, IEEE division) and the same shared-memory stack encoding:
+//   word 0  sorted candidate list, 4 x (octet | source << 3) in 5-bit fields,
+//           length in bits 20-22, next index in bits 23-25;
+//   word 1  the level's static node index;
+//   word 2  the level's dynamic node index (only with a dynamic tree).
+#pragma once
+
+#include "trace.cuh"
+
+namespace qbc {
+
+enum : int { kRunning = 3 };
+
+template <bool EXACT, bool DYN>
+struct Walker {
+  float3 p, d;   // ray origin and direction
+  float4 e0;     // entry point of the basecube
+  float4 cube;   // current cube (tlf.xyz, edge)
+  float4 e;      // entry point of the current cube
+  int level;
+  int32_t ns, nd;
+  int pushes;
+  bool oob;
+  uint32_t vis_s, vis_d;
+
+  static constexpr int kWords = DYN ? 3 : 2;
+
+  __device__ __forceinline__ uint32_t& slot(const Stack& st, int l, int k) const {
+    return st.base[(kWords * l + k) * st.stride];
+  }
+
+  // Basecube entry (octree_fsh.c:157-211). Returns kDiscard or kRunning.
+  __device__ __forceinline__ int start(float4 bc, float3 rp, float3 rd) {
+    p = rp;
+    d = rd;
+    cube = bc;
+    level = 0;
+    ns = 0;
+    nd = 0;
+    pushes = 0;
+    oob = false;
+    vis_s = 0;
+    vis_d = 0;
+    float4 cb = brb_of(bc);
+    int hitc = 0;
+    float4 h0 = make_float4(0.f, 0.f, 0.f, 0.f), h1 = h0, a;
+#define QB_FACE(expr, test)     \
+  a = expr;                     \
+  if (test) {                   \
+    if (hitc == 0) h0 = a;      \
+    else if (hitc == 1) h1 = a; \
+    ++hitc;                     \
+  }
+    QB_FACE(hit_zplane(bc.z, p, d), in_zface(a, bc, cb))  // front
+    QB_FACE(hit_zplane(cb.z, p, d), in_zface(a, bc, cb))  // back
+    QB_FACE(hit_xplane(bc.x, p, d), in_xface(a, bc, cb))  // left
+    QB_FACE(hit_xplane(cb.x, p, d), in_xface(a, bc, cb))  // right
+    QB_FACE(hit_yplane(bc.y, p, d), in_yface(a, bc, cb))  // top
+    QB_FACE(hit_yplane(cb.y, p, d), in_yface(a, bc, cb))  // bottom
+#undef QB_FACE
+    if (hitc < 2 || (h0.w < 0.0f && h1.w < 0.0f)) return kDiscard;
+    if (h1.w < h0.w) h0 = h1;
+    if (h0.w < 0.0f) h0 = make_float4(p.x, p.y, p.z, 0.0f);
+    e0 = h0;
+    e = h0;
+    return kRunning;
+  }
+
+  // Cube and entry point of level lv replayed from the root along the path.
+  __device__ __forceinline__ void replay_to(const Stack& st, int lv, float4 bc, float4& c, float4& en) const {
+    c = bc;
+    en = e0;
+    for (int k = 0; k < lv; ++k) {
+      uint32_t pk = slot(st, k, 0);
+      int cc = list_entry(pk, list_next(pk) - 1);
+      if (cc >> 3) en = plane_point(cc >> 3, c, p, d);
+      c = child_cube(c, cc & 7);
+    }
+  }
+
+  // One step: the subnode test of the current (freshly entered) cube, then
+  // either the descent into its nearest candidate or pops up to the nearest
+  // level with candidates left and the descent into the next one there.
+  // Every step of every lane thus runs exactly one subnode test, so the
+  // lanes of a warp stay on the same instructions for the expensive part.
+  // Returns kRunning, kLeaf (fields via leaf()) or kMiss.
+  __device__ __forceinline__ int step(const DevScene& sc, int maxlevel, float4 bc, const Stack& st) {
+    if (level == maxlevel) return kLeaf;
+
+    // ---- subnode test (octree_fsh.c:251-329) ----
+    int4 s0, s1, d0, d1;
+    if (load_block(sc.tree[0], ns, level, s0, s1, oob)) ++vis_s;
+    if (DYN) {
+      if (load_block(sc.tree[1], nd, level, d0, d1, oob)) ++vis_d;
+    }
+    float4 cb = brb_of(cube);
+    float3 hl = hlf_of(cube);
+    float4 hz = hit_zplane(hl.z, p, d);
+    float4 hx = hit_xplane(hl.x, p, d);
+    float4 hy = hit_yplane(hl.y, p, d);
+    bool vz = hz.w > 0.0f && in_zface(hz, cube, cb);
+    bool vx = hx.w > 0.0f && in_xface(hx, cube, cb);
+    bool vy = hy.w > 0.0f && in_yface(hy, cube, cb);
+
+    // Candidates in the shader's fill order (entry, z, x, y), compacted, as
+    // (t, code): code = octet side bits | source << 3. A bisecting-plane hit
+    // lies on its own plane (its coordinate is the midpoint itself), so its
+    // side bit on that axis is 0. Unused slots hold t = +inf: a valid
+    // candidate has a finite t, so the ordering below never swaps a pad.
+    const float kInf = __int_as_float(0x7f800000);
+    float t[4];
+    uint32_t c[4];
+    t[0] = e.w;
+    c[0] = (e.x > hl.x ? 1u : 0u) | (e.y < hl.y ? 2u : 0u) | (e.z < hl.z ? 4u : 0u);
+    t[1] = t[2] = t[3] = kInf;
+    c[1] = c[2] = c[3] = 0u;
+    int hc = 1;
+    if (vz) {
+      t[1] = hz.w;
+      c[1] = (hz.x > hl.x ? 1u : 0u) | (hz.y < hl.y ? 2u : 0u) | (1u << 3);
+      hc = 2;
+    }
+    if (vx) {
+      float tv = hx.w;
+      uint32_t cv = (hx.y < hl.y ? 2u : 0u) | (hx.z < hl.z ? 4u : 0u) | (2u << 3);
+      if (hc == 1) {
+        t[1] = tv;
+        c[1] = cv;
+      } else {
+        t[2] = tv;
+        c[2] = cv;
+      }
+      ++hc;
+    }
+    if (vy) {
+      float tv = hy.w;
+      uint32_t cv = (hy.x > hl.x ? 1u : 0u) | (hy.z < hl.z ? 4u : 0u) | (3u << 3);
+      if (hc == 1) {
+        t[1] = tv;
+        c[1] = cv;
+      } else if (hc == 2) {
+        t[2] = tv;
+        c[2] = cv;
+      } else {
+        t[3] = tv;
+        c[3] = cv;
+      }
+      ++hc;
+    }
+    // ordering by swaps, as the shader's nested loop (:276-290)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+      for (int j = i + 1; j < 4; ++j) {
+        if (t[j] < t[i]) {
+          float tt = t[i];
+          t[i] = t[j];
+          t[j] = tt;
+          uint32_t cc = c[i];
+          c[i] = c[j];
+          c[j] = cc;
+        }
+      }
+    }
+    // occupied octets: a child in either tree (:313-317)
+    uint32_t occ = 0;
+#pragma unroll
+    for (int o = 0; o < 8; ++o) {
+      bool has = pick8(s0, s1, o) > 0;
+      if (DYN) has = has || pick8(d0, d1, o) > 0;
+      occ |= has ? (1u << o) : 0u;
+    }
+    uint32_t pk = 0;
+    int len = 0, pre = -1;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (i < hc) {
+        int oct = c[i] & 7;
+        const uint32_t src = c[i] >> 3;
+        if (oct == pre) {
+          // pair fix-up for a point on a bisecting plane (:301-309); rare,
+          // so the equality tests are made only here
+          float4 a = src == 0 ? e : (src == 1 ? hz : (src == 2 ? hx : hy));
+          if (a.x == hl.x)
+            oct ^= 1;
+          else if (a.y == hl.y)
+            oct ^= 2;
+          else if (a.z == hl.z)
+            oct ^= 4;
+        }
+        pre = oct;
+        if ((occ >> oct) & 1u) {
+          pk |= (uint32_t)(oct | (src << 3)) << (5 * len);
+          ++len;
+        }
+      }
+    }
+    pk |= (uint32_t)len << 20;
+
+    int nx = 0;
+    float4 isp;
+    int32_t cs, cd = 0;
+    int cc;
+    if (len > 0) {
+      // ---- descend into the nearest candidate (:334-367) ----
+      cc = pk & 31;
+      int src = cc >> 3;
+      isp = src == 0 ? e : (src == 1 ? hz : (src == 2 ? hx : hy));
+      cs = pick8(s0, s1, cc & 7);
+      if (DYN) cd = pick8(d0, d1, cc & 7);
+      slot(st, level, 1) = (uint32_t)ns;
+      if (DYN) slot(st, level, 2) = (uint32_t)nd;
+    } else {
+      // ---- pop until a level has candidates left (:368-375) ----
+      for (;;) {
+        if (level == 0) return kMiss;
+        --level;
+        pk = slot(st, level, 0);
+        nx = list_next(pk);
+        if (EXACT) cube = parent_cube(cube, list_entry(pk, nx - 1) & 7);
+        if (nx < list_len(pk)) break;
+      }
+      cc = list_entry(pk, nx);
+      int src = cc >> 3;
+      if (!EXACT || src == 0) {
+        float4 rc, re;
+        replay_to(st, level, bc, rc, re);
+        cube = rc;
+        isp = re;
+      }
+      if (src != 0) isp = plane_point(src, cube, p, d);
+      int32_t ps = (int32_t)slot(st, level, 1);
+      cs = load_child(sc.tree[0], ps, level, cc & 7, oob);
+      if (DYN) {
+        int32_t pd = (int32_t)slot(st, level, 2);
+        cd = load_child(sc.tree[1], pd, level, cc & 7, oob);
+      }
+    }
+    if (++pushes > kMaxPushes) {
+      oob = true;
+      return kMiss;
+    }
+    slot(st, level, 0) = (pk & ~(7u << 23)) | ((uint32_t)(nx + 1) << 23);
+    cube = child_cube(cube, cc & 7);
+    e = isp;
+    ns = cs;
+    nd = cd;
+    ++level;
+    return kRunning;
+  }
+
+  // Leaf fetch (octree_fsh.c:218-247); call after step() returned kLeaf.
+  __device__ __forceinline__ void leaf(const DevScene& sc, int32_t& ms, int32_t& md, float4& col, float4& nrm) {
+    ms = load_model(sc.tree[0], ns, level, oob);
+    md = DYN ? load_model(sc.tree[1], nd, level, oob) : 0;
+    load_attr(sc.model[0], ms, col, nrm, oob);
+    if (DYN && md > 0) load_attr(sc.model[1], md, col, nrm, oob);
+  }
+};
+
+}  // namespace qbc
