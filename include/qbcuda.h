@@ -193,6 +193,33 @@ typedef struct qbc_ray_hits
 
 int qbc_trace_rays(qbc_ctx* ctx, const float* pos, const float* dir, int64_t n, const float basecube[4], int maxlevel, const qbc_ray_hits* out, int on_device);
 
+/*
+ * Render without allocating anything (no counterpart in the reference).
+ *
+ * For callers that cannot call cudaMalloc while they render: a frame loop
+ * that must not stall on an allocation (cudaMalloc and cudaFree can
+ * synchronize the device), a process whose device memory is already handed
+ * to another allocator or a fixed budget, or code that must keep the
+ * device's allocation state unchanged between frames. Same pixels as
+ * qbc_render_views with device outputs; the caller passes the views and
+ * DEVICE output buffers on the context's GPU, the scene comes from earlier
+ * qbc_upload calls, and the work is queued on the context's stream.
+ *
+ * The only scratch the kernel needs, its work-queue counters, lives in a
+ * fixed array of QBC_NOALLOC_MAX_LAUNCHES counters in the library's static
+ * device memory, held by every GPU that loads the library until exit. A call
+ * takes one counter per 32 views, so at most QBC_NOALLOC_MAX_VIEWS views per
+ * call; more is rejected with QBC_E_ARG. The counters are cleared on the
+ * stream before each use. All calls share them: two calls whose work
+ * overlaps on the GPU (different streams, different contexts on one device)
+ * race and must be ordered by the caller. The first call on a device looks
+ * up the array's device address; make that first call before any stream
+ * capture. Host output pointers are rejected with QBC_E_ARG.
+ */
+#define QBC_NOALLOC_MAX_LAUNCHES 8
+#define QBC_NOALLOC_MAX_VIEWS (QBC_NOALLOC_MAX_LAUNCHES * 32)
+int qbc_render_views_noalloc(qbc_ctx* ctx, const qbc_view* views, const qbc_outputs* outs, int n);
+
 /* Run the context's work on this CUDA stream (a cudaStream_t; NULL = the
  * context's own stream). */
 int qbc_set_stream(qbc_ctx* ctx, void* stream);

@@ -20,6 +20,7 @@ QBC_GL_FLOAT = 0x1406
 
 STATIC_COLOR, STATIC_NORMAL, STATIC_OCTREE, DYNAMIC_COLOR, DYNAMIC_NORMAL, DYNAMIC_OCTREE = range(6)
 MAX_LEVEL = 17
+NOALLOC_MAX_VIEWS = 256
 
 PX_PRIMARY_LEAF = 1 << 0
 PX_DISCARD = 1 << 1
@@ -132,6 +133,7 @@ SIGNATURES = {
     "qbc_render_views": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int, C.c_int]),
     "qbc_trace_rays": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, c_float_p, C.c_int,
                                  C.POINTER(RayHits), C.c_int]),
+    "qbc_render_views_noalloc": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int]),
     "qbc_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "qbc_synchronize": (C.c_int, [C.c_void_p]),
     "qbc_tree_nodes": (C.c_int, [C.c_void_p, C.c_int, c_int64_p]),

@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "qbc_internal.h"
@@ -525,6 +526,117 @@ extern "C" int qbc_trace_rays(qbc_ctx* c, const float* pos, const float* dir, in
     for (int k = 0; k < 7; ++k)
       if (*hs[k]) QBC_CUDA(cudaMemcpyAsync(*hs[k], dv[k], (size_t)n * bytes[k], cudaMemcpyDeviceToHost, c->stream));
     QBC_CUDA(cudaStreamSynchronize(c->stream));
+  }
+  return QBC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Render without allocating (qbc_render_views_noalloc)
+// ---------------------------------------------------------------------------
+
+// Work-queue counters of qbc_render_views_noalloc: one per launch of 32
+// views. File-scope static device memory, so the call needs no allocation;
+// every GPU that loads the library holds these 256 bytes until exit.
+static __device__ __align__(256) unsigned int qbc_noalloc_queues[QBC_NOALLOC_MAX_LAUNCHES];
+
+namespace {
+
+constexpr int kNoallocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned int* g_noalloc_ptr[kNoallocMaxDevices] = {};
+
+// Device address of the counters on the current device, looked up once per
+// device (cudaGetSymbolAddress with that device current).
+int noalloc_queues(int device, unsigned int** out) {
+  if (device < 0 || device >= kNoallocMaxDevices)
+    return fail(QBC_E_ARG, "qbc_render_views_noalloc: device %d beyond %d", device, kNoallocMaxDevices);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[device]) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, qbc_noalloc_queues);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(qbc_noalloc_queues)");
+    g_noalloc_ptr[device] = static_cast<unsigned int*>(ptr);
+  }
+  *out = g_noalloc_ptr[device];
+  return QBC_OK;
+}
+
+template <bool EXACT, bool DYN>
+int launch_render_noalloc(qbc_ctx* c, const qbc::Batch& b, size_t smem, unsigned int* queue) {
+  auto kern = qbc::render_kernel<EXACT, DYN>;
+  QBC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+  int per_sm = 0;
+  QBC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, qbc::kThreads, smem));
+  if (per_sm < 1) return fail(QBC_E_STATE, "render_kernel: no block fits on an SM with %zu B shared memory", smem);
+  int64_t blocks = std::min<int64_t>((int64_t)per_sm * c->sm_count, ((int64_t)b.tiles_total + 3) / 4);
+  blocks = std::max<int64_t>(blocks, 1);
+  kern<<<(unsigned)blocks, qbc::kThreads, smem, c->stream>>>(device_scene(c), b, queue);
+  QBC_CUDA(cudaGetLastError());
+  ++c->launches;
+  return QBC_OK;
+}
+
+}  // namespace
+
+extern "C" int qbc_render_views_noalloc(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs, int n) {
+  qbc::clear_error();
+  if (!c || (n > 0 && (!views || !outs))) return fail(QBC_E_ARG, "qbc_render_views_noalloc: null argument");
+  if (n < 0) return fail(QBC_E_ARG, "qbc_render_views_noalloc: negative view count");
+  if (n > QBC_NOALLOC_MAX_VIEWS)
+    return fail(QBC_E_ARG, "qbc_render_views_noalloc: %d views exceed the maximum of %d per call (%d work-queue counters of 32 views)",
+                n, QBC_NOALLOC_MAX_VIEWS, QBC_NOALLOC_MAX_LAUNCHES);
+  if (n == 0) return QBC_OK;
+  QBC_CUDA(cudaSetDevice(c->device));
+  for (int i = 0; i < n; ++i) {
+    int rc = check_view(views[i], i);
+    if (rc) return rc;
+    const qbc_outputs& o = outs[i];
+    const void* ptrs[6] = {o.rgba8, o.rgba32f, o.flags, o.leaf, o.isp, o.visits};
+    for (int k = 0; k < 6; ++k) {
+      if (!ptrs[k]) continue;
+      cudaPointerAttributes attr;
+      cudaError_t e = cudaPointerGetAttributes(&attr, ptrs[k]);
+      if (e != cudaSuccess || attr.type != cudaMemoryTypeDevice || attr.device != c->device) {
+        cudaGetLastError();
+        return fail(QBC_E_ARG, "qbc_render_views_noalloc: output %d of view %d is not device memory of device %d", k,
+                    i, c->device);
+      }
+    }
+  }
+  unsigned int* queues = nullptr;
+  int rc = noalloc_queues(c->device, &queues);
+  if (rc) return rc;
+  const int launches = (n + qbc::kMaxViewsPerLaunch - 1) / qbc::kMaxViewsPerLaunch;
+  // the counters keep the previous call's values: start every used one at 0
+  QBC_CUDA(cudaMemsetAsync(queues, 0, sizeof(unsigned int) * (size_t)launches, c->stream));
+  const bool dyn = c->tree[1].n > 0;
+  qbc::Batch b;  // on the stack: no host allocation either
+  for (int l = 0; l < launches; ++l) {
+    const int a = l * qbc::kMaxViewsPerLaunch;
+    const int m = std::min(qbc::kMaxViewsPerLaunch, n - a);
+    std::memset(&b, 0, sizeof(b));
+    int tiles = 0, maxlevel = 0;
+    bool exact = true;
+    for (int i = 0; i < m; ++i) {
+      qbc::ViewJob& J = b.job[i];
+      J.v = views[a + i];
+      J.o = outs[a + i];
+      J.tiles_x = (views[a + i].width_px + 7) / 8;
+      J.tile_begin = tiles;
+      tiles += J.tiles_x * ((views[a + i].height_px + 3) / 4);
+      maxlevel = std::max(maxlevel, views[a + i].maxlevel);
+      exact = exact && qbc::cube_shift_exact(views[a + i]);
+    }
+    b.n = m;
+    b.tiles_total = tiles;
+    b.max_level = maxlevel;
+    const size_t smem = ((size_t)(dyn ? 3 : 2) * maxlevel + qbc::kPixWords) * qbc::kThreads * sizeof(uint32_t);
+    unsigned int* q = queues + l;
+    if (exact)
+      rc = dyn ? launch_render_noalloc<true, true>(c, b, smem, q) : launch_render_noalloc<true, false>(c, b, smem, q);
+    else
+      rc = dyn ? launch_render_noalloc<false, true>(c, b, smem, q) : launch_render_noalloc<false, false>(c, b, smem, q);
+    if (rc) return rc;
   }
   return QBC_OK;
 }

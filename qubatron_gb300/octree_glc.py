@@ -133,6 +133,14 @@ class OctreeGLC:
         oarr = (Outputs * n)(*outputs)
         check(self._lib.qbc_render_views(self.handle, varr, oarr, n, 1 if on_device else 0))
 
+    def render_views_noalloc(self, views: Sequence[View], outputs: Sequence[Outputs]) -> None:
+        """qbc_render_views_noalloc: device outputs only, no allocation in
+        the call (the work-queue counters live in static device memory)."""
+        n = len(views)
+        varr = (View * n)(*views)
+        oarr = (Outputs * n)(*outputs)
+        check(self._lib.qbc_render_views_noalloc(self.handle, varr, oarr, n))
+
     def render_host(self, views: Sequence[View], streams: Iterable[str] = ("rgba8",)) -> list:
         """Render views into fresh numpy buffers; returns a FrameBuffers per view."""
         bufs = [FrameBuffers(v, streams) for v in views]
