@@ -239,6 +239,8 @@ def run_gpu(args):
     ctx.set_stream(stream.cuda_stream)
     ctx.upload_model(False, scene.colors, scene.normals)
     ctx.upload_octree(False, scene.nodes)
+    if args.service_min:
+        ctx.set_option(qb._lib.OPT_SERVICE_MIN, args.service_min)
 
     # device outputs
     frames = [torch.empty((v.height_px, v.width_px, 4), dtype=torch.uint8, device="cuda") for v in views]
@@ -357,6 +359,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--service-min", type=int, default=0, help="override the kernel's service threshold")
     ap.add_argument("--workload", default=None)
     args = ap.parse_args()
     global WORKLOAD

@@ -225,6 +225,16 @@ int qbc_render_views_noalloc(qbc_ctx* ctx, const qbc_view* views, const qbc_outp
 int qbc_set_stream(qbc_ctx* ctx, void* stream);
 int qbc_synchronize(qbc_ctx* ctx);
 
+/*
+ * Tuning options of a context (performance only; results do not change).
+ *   QBC_OPT_SERVICE_MIN  1..32, default 4: in the persistent render kernel a
+ *   lane whose ray ended waits until this many lanes of its warp wait (or no
+ *   ray runs) before the warp starts their next rays together.
+ */
+#define QBC_OPT_SERVICE_MIN 1
+int qbc_set_option(qbc_ctx* ctx, int option, int value);
+int qbc_get_option(qbc_ctx* ctx, int option, int* value);
+
 /* Node and point counts currently held for a tree / model (0 static, 1 dynamic). */
 int qbc_tree_nodes(qbc_ctx* ctx, int tree, int64_t* n_nodes);
 int qbc_model_points(qbc_ctx* ctx, int model, int64_t* n_points);

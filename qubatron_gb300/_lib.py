@@ -136,6 +136,8 @@ SIGNATURES = {
     "qbc_render_views_noalloc": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int]),
     "qbc_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "qbc_synchronize": (C.c_int, [C.c_void_p]),
+    "qbc_set_option": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "qbc_get_option": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
     "qbc_tree_nodes": (C.c_int, [C.c_void_p, C.c_int, c_int64_p]),
     "qbc_model_points": (C.c_int, [C.c_void_p, C.c_int, c_int64_p]),
     "qbc_launch_count": (C.c_int, [C.c_void_p, c_int64_p]),
@@ -152,8 +154,13 @@ SIGNATURES = {
 _LIB = None
 
 
+OPT_SERVICE_MIN = 1
+
+
 def lib_path() -> str:
-    return _build.LIB
+    """The in-tree build, or the file named by QBC_LIBRARY (another build of
+    the same library, e.g. one compiled with different tuning)."""
+    return os.environ.get("QBC_LIBRARY") or _build.LIB
 
 
 def load(build_if_missing: bool = True) -> C.CDLL:
@@ -162,7 +169,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     if _LIB is not None:
         return _LIB
     path = lib_path()
-    if build_if_missing:
+    if build_if_missing and path == _build.LIB:
         _build.build()
     if not os.path.exists(path):
         raise QbcError(-4, f"libqbcuda.so not built at {path}")

@@ -71,6 +71,7 @@ struct qbc_ctx {
   unsigned int* queue = nullptr;  // global tile counter of the persistent render kernel
   int render_blocks[4] = {0, 0, 0, 0};  // resident blocks per SM of each render_kernel variant
   int attr_done = 0;
+  int service_min = qbc::kServiceMinDefault;
   int64_t launches = 0;
 };
 
@@ -123,12 +124,12 @@ qbc::DevScene device_scene(const qbc_ctx* c) {
   for (int t = 0; t < 2; ++t) {
     s.tree[t].child = c->tree[t].child;
     s.tree[t].model = c->tree[t].model;
-    s.tree[t].n = c->tree[t].n;
+    s.tree[t].n = (int32_t)c->tree[t].n;
     s.model[t].col = c->model[t].col;
     s.model[t].nrm = c->model[t].nrm;
     // the colour and normal arrays are separate uploads; a point index is
     // valid when both hold it
-    s.model[t].n = std::min(c->model[t].n_col, c->model[t].n_nrm);
+    s.model[t].n = (int32_t)std::min(c->model[t].n_col, c->model[t].n_nrm);
   }
   return s;
 }
@@ -184,6 +185,25 @@ extern "C" int qbc_set_stream(qbc_ctx* c, void* stream) {
   if (!c) return fail(QBC_E_ARG, "qbc_set_stream: null context");
   c->stream = stream ? (cudaStream_t)stream : c->own;
   return QBC_OK;
+}
+
+extern "C" int qbc_set_option(qbc_ctx* c, int option, int value) {
+  if (!c) return fail(QBC_E_ARG, "qbc_set_option: null context");
+  if (option == QBC_OPT_SERVICE_MIN) {
+    if (value < 1 || value > 32) return fail(QBC_E_ARG, "qbc_set_option: service threshold %d outside 1..32", value);
+    c->service_min = value;
+    return QBC_OK;
+  }
+  return fail(QBC_E_ARG, "qbc_set_option: unknown option %d", option);
+}
+
+extern "C" int qbc_get_option(qbc_ctx* c, int option, int* value) {
+  if (!c || !value) return fail(QBC_E_ARG, "qbc_get_option: null argument");
+  if (option == QBC_OPT_SERVICE_MIN) {
+    *value = c->service_min;
+    return QBC_OK;
+  }
+  return fail(QBC_E_ARG, "qbc_get_option: unknown option %d", option);
 }
 
 extern "C" int qbc_synchronize(qbc_ctx* c) {
@@ -367,6 +387,7 @@ int launch_batch(qbc_ctx* c, const qbc_view* views, const qbc_outputs* dev_outs,
   b->n = n;
   b->tiles_total = tiles;
   b->max_level = maxlevel;
+  b->service_min = c->service_min;
   const bool dyn = c->tree[1].n > 0;
   const size_t words = (size_t)(dyn ? 3 : 2) * maxlevel + qbc::kPixWords;
   const size_t smem = words * qbc::kThreads * sizeof(uint32_t);
@@ -630,6 +651,7 @@ extern "C" int qbc_render_views_noalloc(qbc_ctx* c, const qbc_view* views, const
     b.n = m;
     b.tiles_total = tiles;
     b.max_level = maxlevel;
+    b.service_min = c->service_min;
     const size_t smem = ((size_t)(dyn ? 3 : 2) * maxlevel + qbc::kPixWords) * qbc::kThreads * sizeof(uint32_t);
     unsigned int* q = queues + l;
     if (exact)

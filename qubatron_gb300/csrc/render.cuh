@@ -30,8 +30,8 @@ struct Batch {
   ViewJob job[kMaxViewsPerLaunch];
   int32_t n;
   int32_t tiles_total;
-  int32_t max_level;  // largest maxlevel of the batch: stack depth
-  int32_t pad;
+  int32_t max_level;    // largest maxlevel of the batch: stack depth
+  int32_t service_min;  // lanes that must wait before a warp services them
 };
 
 // ---- main() helpers (octree_fsh.c:381-395 and GLSL built-ins) ----
@@ -286,10 +286,11 @@ __device__ __forceinline__ int tile_view(const Batch& b, int tile) {
   return lo;
 }
 
-// Lanes whose ray ended wait until at least this many lanes of the warp need
-// service (or no ray is left running); then ray transitions, refills and ray
-// starts run for all of them together instead of one lane at a time.
-constexpr int kServiceMin = 8;
+// Lanes whose ray ended wait until at least batch.service_min lanes of the
+// warp need service (or no ray is left running); then ray transitions,
+// refills and ray starts run for all of them together instead of one lane at
+// a time.
+constexpr int kServiceMinDefault = 4;
 
 template <bool EXACT, bool DYN>
 __global__ void __launch_bounds__(kThreads) render_kernel(DevScene sc, const __grid_constant__ Batch batch,
@@ -310,7 +311,7 @@ __global__ void __launch_bounds__(kThreads) render_kernel(DevScene sc, const __g
   for (;;) {
     const unsigned run = __ballot_sync(0xFFFFFFFFu, S.running);
     const int waiting = 32 - __popc(run);
-    if (run == 0 || waiting >= kServiceMin) {
+    if (run == 0 || waiting >= batch.service_min) {
       // ---- service: consume ended rays, refill, start new rays together ----
       float3 rp = make_float3(0.f, 0.f, 0.f), rd = rp;
       bool go = false;

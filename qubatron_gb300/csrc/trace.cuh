@@ -34,13 +34,13 @@ constexpr int kMaxPushes = 1 << 22;
 struct DevTree {
   const int4* child;     // 2 int4 per node: the 8 child indices
   const int32_t* model;  // slot 8: model index of the point that made the node
-  int64_t n;             // nodes held; index >= n reads as 0 and is reported
+  int32_t n;             // nodes held; index >= n reads as 0 and is reported
 };
 
 struct DevModel {
   const float4* col;  // (r, g, b, 1) per point, as an RGB32F texel reads
   const float4* nrm;  // (x, y, z, 1)
-  int64_t n;
+  int32_t n;
 };
 
 struct DevScene {
@@ -51,47 +51,39 @@ struct DevScene {
 enum : int { kMiss = 0, kLeaf = 1, kDiscard = 2 };
 
 
-// ---- is_cube_{x,y,z}plane (octree_fsh.c:62-99) ----
+// ---- is_cube_{x,y,z}plane (octree_fsh.c:62-99), branch-free ----
+// A ray parallel to the plane gets FLT_MAX in every component, as in the
+// shader; the division then runs on a dummy divisor of 1 and its result is
+// replaced, so any other ray gets exactly (c - p) / d and p + d * t.
 __device__ __forceinline__ float4 hit_xplane(float x, float3 p, float3 d) {
-  float4 r = make_float4(kFltMax, kFltMax, kFltMax, kFltMax);
-  if (d.x != 0.0f) {
-    r.w = (x - p.x) / d.x;
-    r.y = p.y + d.y * r.w;
-    r.z = p.z + d.z * r.w;
-    r.x = x;
-  }
-  return r;
+  const bool par = d.x == 0.0f;
+  const float w = (x - p.x) / (par ? 1.0f : d.x);
+  return make_float4(par ? kFltMax : x, par ? kFltMax : p.y + d.y * w, par ? kFltMax : p.z + d.z * w,
+                     par ? kFltMax : w);
 }
 __device__ __forceinline__ float4 hit_yplane(float y, float3 p, float3 d) {
-  float4 r = make_float4(kFltMax, kFltMax, kFltMax, kFltMax);
-  if (d.y != 0.0f) {
-    r.w = (y - p.y) / d.y;
-    r.x = p.x + d.x * r.w;
-    r.z = p.z + d.z * r.w;
-    r.y = y;
-  }
-  return r;
+  const bool par = d.y == 0.0f;
+  const float w = (y - p.y) / (par ? 1.0f : d.y);
+  return make_float4(par ? kFltMax : p.x + d.x * w, par ? kFltMax : y, par ? kFltMax : p.z + d.z * w,
+                     par ? kFltMax : w);
 }
 __device__ __forceinline__ float4 hit_zplane(float z, float3 p, float3 d) {
-  float4 r = make_float4(kFltMax, kFltMax, kFltMax, kFltMax);
-  if (d.z != 0.0f) {
-    r.w = (z - p.z) / d.z;
-    r.x = p.x + d.x * r.w;
-    r.y = p.y + d.y * r.w;
-    r.z = z;
-  }
-  return r;
+  const bool par = d.z == 0.0f;
+  const float w = (z - p.z) / (par ? 1.0f : d.z);
+  return make_float4(par ? kFltMax : p.x + d.x * w, par ? kFltMax : p.y + d.y * w, par ? kFltMax : z,
+                     par ? kFltMax : w);
 }
 
-// Half-open face tests (octree_fsh.c:166-192, 263-271).
+// Half-open face tests (octree_fsh.c:166-192, 263-271), evaluated without
+// short-circuit branches.
 __device__ __forceinline__ bool in_zface(float4 a, float4 t, float4 b) {
-  return t.x < a.x && a.x <= b.x && t.y > a.y && a.y >= b.y;
+  return (t.x < a.x) & (a.x <= b.x) & (t.y > a.y) & (a.y >= b.y);
 }
 __device__ __forceinline__ bool in_xface(float4 a, float4 t, float4 b) {
-  return t.y > a.y && a.y >= b.y && t.z > a.z && a.z >= b.z;
+  return (t.y > a.y) & (a.y >= b.y) & (t.z > a.z) & (a.z >= b.z);
 }
 __device__ __forceinline__ bool in_yface(float4 a, float4 t, float4 b) {
-  return t.x < a.x && a.x <= b.x && t.z > a.z && a.z >= b.z;
+  return (t.x < a.x) & (a.x <= b.x) & (t.z > a.z) & (a.z >= b.z);
 }
 
 __device__ __forceinline__ float4 brb_of(float4 t) {
@@ -140,49 +132,50 @@ __device__ __forceinline__ int32_t pick8(int4 a, int4 b, int o) {
 }
 
 // Child block of node i (oct_from_octets_for_index, octree_fsh.c:127-136):
-// node 0 below the root is "no node"; a tree never uploaded holds nothing.
+// node 0 below the root is "no node"; a tree never uploaded holds nothing; an
+// index outside the array reads as empty and is reported. One unsigned
+// compare covers negative and too-large indices.
 __device__ __forceinline__ bool load_block(const DevTree& t, int32_t i, int level, int4& a, int4& b,
                                            bool& oob) {
+  const bool none = ((i == 0) & (level > 0)) | (t.n == 0);
+  const bool bad = !none & ((uint32_t)i >= (uint32_t)t.n);
+  oob |= bad;
   a = make_int4(0, 0, 0, 0);
   b = a;
-  if ((i == 0 && level > 0) || t.n == 0) return false;
-  if (i < 0 || (int64_t)i >= t.n) {
-    oob = true;
-    return false;
+  if (!none & !bad) {
+    a = __ldg(t.child + 2 * (uint32_t)i);
+    b = __ldg(t.child + 2 * (uint32_t)i + 1);
+    return true;
   }
-  a = __ldg(t.child + 2 * (int64_t)i);
-  b = __ldg(t.child + 2 * (int64_t)i + 1);
-  return true;
+  return false;
 }
 
 __device__ __forceinline__ int32_t load_child(const DevTree& t, int32_t i, int level, int o, bool& oob) {
-  if ((i == 0 && level > 0) || t.n == 0) return 0;
-  if (i < 0 || (int64_t)i >= t.n) {
-    oob = true;
-    return 0;
-  }
-  return __ldg(reinterpret_cast<const int32_t*>(t.child) + 8 * (int64_t)i + o);
+  const bool none = ((i == 0) & (level > 0)) | (t.n == 0);
+  const bool bad = !none & ((uint32_t)i >= (uint32_t)t.n);
+  oob |= bad;
+  if (none | bad) return 0;
+  return __ldg(reinterpret_cast<const int32_t*>(t.child) + 8 * (uint32_t)i + o);
 }
 
 __device__ __forceinline__ int32_t load_model(const DevTree& t, int32_t i, int level, bool& oob) {
-  if ((i == 0 && level > 0) || t.n == 0) return 0;
-  if (i < 0 || (int64_t)i >= t.n) {
-    oob = true;
-    return 0;
-  }
-  return __ldg(t.model + i);
+  const bool none = ((i == 0) & (level > 0)) | (t.n == 0);
+  const bool bad = !none & ((uint32_t)i >= (uint32_t)t.n);
+  oob |= bad;
+  if (none | bad) return 0;
+  return __ldg(t.model + (uint32_t)i);
 }
 
 __device__ __forceinline__ void load_attr(const DevModel& m, int32_t i, float4& col, float4& nrm, bool& oob) {
   col = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   nrm = col;
   if (m.n == 0) return;
-  if (i < 0 || (int64_t)i >= m.n) {
+  if ((uint32_t)i >= (uint32_t)m.n) {
     oob = true;
     return;
   }
-  col = __ldg(m.col + i);
-  nrm = __ldg(m.nrm + i);
+  col = __ldg(m.col + (uint32_t)i);
+  nrm = __ldg(m.nrm + (uint32_t)i);
 }
 
 // Per-thread stack in shared memory: word k of level l at st[(3 * l + k) * stride].

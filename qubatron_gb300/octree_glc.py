@@ -165,6 +165,14 @@ class OctreeGLC:
     def set_stream(self, stream_ptr: Optional[int]) -> None:
         check(self._lib.qbc_set_stream(self.handle, C.c_void_p(stream_ptr or 0)))
 
+    def set_option(self, option: int, value: int) -> None:
+        check(self._lib.qbc_set_option(self.handle, int(option), int(value)))
+
+    def get_option(self, option: int) -> int:
+        v = C.c_int()
+        check(self._lib.qbc_get_option(self.handle, int(option), C.byref(v)))
+        return v.value
+
     def synchronize(self) -> None:
         check(self._lib.qbc_synchronize(self.handle))
 
