@@ -242,6 +242,24 @@ int qbc_model_points(qbc_ctx* ctx, int model, int64_t* n_points);
 /* Kernel launches issued by this context since creation. */
 int qbc_launch_count(qbc_ctx* ctx, int64_t* count);
 
+/*
+ * GPU tree build into the context's static (tree 0) or dynamic (tree 1)
+ * octree: the node array that inserting the n points in order into an empty
+ * tree gives (octree_reset + octree_insert_point, octree.c:89-147, model
+ * indices first_index + i), numbering included, built with sorts and prefix
+ * sums instead of one walk per point. The result replaces the tree exactly
+ * as a whole-array qbc_upload of that array would. pnts is n float3 on the
+ * host (on_device = 0) or on the context's GPU.
+ */
+int qbc_build_tree(qbc_ctx* ctx, int tree, const float* pnts, int64_t n, float basesize, int levels, int64_t first_index, int on_device);
+/* The same from per-point octet paths, `levels` int32 per point in 0..7
+ * (octree_insert_path, octree.c:149-180; the per-frame dynamic rebuild of
+ * qubatron.c:439-452 from the paths of skeleton_vsh.c:188-213). */
+int qbc_build_tree_paths(qbc_ctx* ctx, int tree, const int32_t* octets, int64_t n, int levels, int64_t first_index, int on_device);
+/* Copy a tree back to the host in the reference layout (12 int32 per node:
+ * 8 children, model index, 3 zero). nodes may be NULL to query the count. */
+int qbc_download_tree(qbc_ctx* ctx, int tree, int32_t* nodes, int64_t cap, int64_t* n_nodes);
+
 /* ---- node-array producer (octree.c:95-218) ---- */
 
 /* A growable host node array (12 int32 per node, node 0 = root). */

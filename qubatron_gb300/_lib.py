@@ -141,6 +141,9 @@ SIGNATURES = {
     "qbc_tree_nodes": (C.c_int, [C.c_void_p, C.c_int, c_int64_p]),
     "qbc_model_points": (C.c_int, [C.c_void_p, C.c_int, c_int64_p]),
     "qbc_launch_count": (C.c_int, [C.c_void_p, c_int64_p]),
+    "qbc_build_tree": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int64, C.c_float, C.c_int, C.c_int64, C.c_int]),
+    "qbc_build_tree_paths": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int64, C.c_int, C.c_int64, C.c_int]),
+    "qbc_download_tree": (C.c_int, [C.c_void_p, C.c_int, c_int32_p, C.c_int64, c_int64_p]),
     "qbc_octree_create": (C.c_int, [C.c_float, C.c_int, C.POINTER(C.c_void_p)]),
     "qbc_octree_free": (C.c_int, [C.c_void_p]),
     "qbc_octree_reset": (C.c_int, [C.c_void_p]),

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libqbcuda.so")
 
-SOURCES = ["qbcuda.cu", "host.cpp"]
+SOURCES = ["qbcuda.cu", "build.cu", "host.cpp"]
 HEADERS = ["trace.cuh", "walker.cuh", "render.cuh", "qbc_internal.h"]
 
 NVCC_FLAGS = [
@@ -47,22 +47,40 @@ def _stale() -> bool:
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile libqbcuda.so if any source is newer; return its path."""
+    """Compile libqbcuda.so if any source is newer; return its path. The
+    translation units compile in parallel, then link into one shared library."""
     if not force and not _stale():
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
+    inc = ["-I", os.path.join(ROOT, "include")]
+    compile_flags = [f for f in NVCC_FLAGS if f != "-shared"]
+    procs = []
+    objs = []
+    for src in SOURCES:
+        obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
+        objs.append(obj)
+        cmd = [_nvcc(), *compile_flags, *inc, "-c", os.path.join(CSRC, src), "-o", obj]
+        if verbose:
+            cmd += ["-Xptxas", "-v"]
+            print(" ".join(cmd), file=sys.stderr)
+        procs.append((src, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)))
+    errors = []
+    for src, p in procs:
+        out, err = p.communicate()
+        if p.returncode != 0:
+            errors.append(f"--- {src}\n{out}{err}")
+        elif verbose:
+            sys.stderr.write(err)
+    if errors:
+        raise RuntimeError("nvcc failed building libqbcuda:\n" + "\n".join(errors))
     tmp = LIB + ".tmp"
-    cmd = [_nvcc(), *NVCC_FLAGS, "-I", os.path.join(ROOT, "include"), "-o", tmp]
-    cmd += [os.path.join(CSRC, f) for f in SOURCES]
-    if verbose:
-        cmd += ["-Xptxas", "-v"]
-        print(" ".join(cmd), file=sys.stderr)
-    res = subprocess.run(cmd, capture_output=True, text=True)
+    link = [_nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-shared", "-Xcompiler", "-fPIC", "-o", tmp, *objs]
+    res = subprocess.run(link, capture_output=True, text=True)
     if res.returncode != 0:
-        raise RuntimeError("nvcc failed building libqbcuda:\n" + res.stdout + res.stderr)
-    if verbose:
-        sys.stderr.write(res.stderr)
+        raise RuntimeError("nvcc failed linking libqbcuda:\n" + res.stdout + res.stderr)
     os.replace(tmp, LIB)
+    for o in objs:
+        os.remove(o)
     return LIB
 
 

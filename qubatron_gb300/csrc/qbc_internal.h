@@ -1,6 +1,10 @@
 // Internal helpers shared by the translation units of libqbcuda.
 #pragma once
 
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
 #include "qbcuda.h"
 
 namespace qbc {
@@ -12,5 +16,22 @@ void clear_error();
 // True when every cube coordinate of the view's traversal is exactly
 // representable, so a child shift can be undone exactly on the way up.
 bool cube_shift_exact(const qbc_view& v);
+
+// Destination of a GPU tree build: grow() must make child (8 int32 per node)
+// and model (1 int32 per node) hold `nodes` nodes on the device.
+struct BuildTarget {
+  int32_t* child;
+  int32_t* model;
+  int64_t n_nodes;
+  int64_t launches;
+  void* user;
+  int (*grow)(BuildTarget* self, int64_t nodes);
+};
+
+// Build the node array of inserting n points (d_pts, float3) or n octet
+// paths (d_octets, `levels` per point) in order into an empty tree. Inputs
+// are device pointers; exactly one of d_pts / d_octets is non-null.
+int build_nodes(const float* d_pts, const int32_t* d_octets, int64_t n, float basesize, int levels,
+                int64_t first_index, cudaStream_t stream, BuildTarget* tgt);
 
 }  // namespace qbc

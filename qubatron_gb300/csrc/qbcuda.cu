@@ -320,6 +320,111 @@ extern "C" int qbc_upload(qbc_ctx* c, const void* data, int type, size_t size, s
 }
 
 // ---------------------------------------------------------------------------
+// GPU tree build (octree_insert_point / octree_insert_path order)
+// ---------------------------------------------------------------------------
+
+namespace {
+
+int grow_tree_target(qbc::BuildTarget* t, int64_t nodes) {
+  DevTreeBuf& tb = *static_cast<DevTreeBuf*>(t->user);
+  if (nodes > tb.cap) {
+    int64_t cap = nodes + nodes / 8;
+    int rc = grow(&tb.child, &tb.cap, cap, 32, "octree child blocks");
+    if (rc) return rc;
+    int64_t mcap = 0;
+    rc = grow(&tb.model, &mcap, cap, 4, "octree model indices");
+    if (rc) return rc;
+  }
+  t->child = reinterpret_cast<int32_t*>(tb.child);
+  t->model = tb.model;
+  return QBC_OK;
+}
+
+int build_into(qbc_ctx* c, int tree, const float* pnts, const int32_t* octets, int64_t n, float basesize, int levels,
+               int64_t first_index, int on_device) {
+  if (!c || tree < 0 || tree > 1) return fail(QBC_E_ARG, "tree build: bad context or tree id");
+  if (n < 0 || (n > 0 && !pnts && !octets)) return fail(QBC_E_ARG, "tree build: bad input");
+  if (pnts && !(basesize > 0.0f)) return fail(QBC_E_ARG, "tree build: basesize must be positive");
+  if (levels < 0 || levels > 21) return fail(QBC_E_ARG, "tree build: levels %d outside 0..21", levels);
+  QBC_CUDA(cudaSetDevice(c->device));
+  const float* dp = pnts;
+  const int32_t* doc = octets;
+  void* tmp = nullptr;
+  if (!on_device && n > 0) {
+    size_t bytes = pnts ? (size_t)n * 12 : (size_t)n * levels * 4;
+    cudaError_t e = cudaMalloc(&tmp, bytes);
+    if (e != cudaSuccess) return fail(QBC_E_NOMEM, "tree build input of %zu bytes: %s", bytes, cudaGetErrorString(e));
+    e = cudaMemcpyAsync(tmp, pnts ? (const void*)pnts : (const void*)octets, bytes, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) {
+      cudaFree(tmp);
+      return cuda_fail(e, "tree build input copy");
+    }
+    if (pnts)
+      dp = static_cast<const float*>(tmp);
+    else
+      doc = static_cast<const int32_t*>(tmp);
+  }
+  qbc::BuildTarget t{nullptr, nullptr, 0, 0, &c->tree[tree], grow_tree_target};
+  int rc = qbc::build_nodes(pnts ? dp : nullptr, pnts ? nullptr : doc, n, basesize, levels, first_index, c->stream, &t);
+  if (tmp) cudaFree(tmp);
+  c->launches += t.launches;
+  if (rc) return rc;
+  c->tree[tree].n = t.n_nodes;
+  return QBC_OK;
+}
+
+__global__ void unpack_nodes_kernel(const int4* __restrict__ child, const int32_t* __restrict__ model, int64_t n,
+                                    int4* __restrict__ raw) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    raw[3 * i] = child[2 * i];
+    raw[3 * i + 1] = child[2 * i + 1];
+    raw[3 * i + 2] = make_int4(model[i], 0, 0, 0);
+  }
+}
+
+}  // namespace
+
+extern "C" int qbc_build_tree(qbc_ctx* c, int tree, const float* pnts, int64_t n, float basesize, int levels,
+                              int64_t first_index, int on_device) {
+  qbc::clear_error();
+  if (n > 0 && !pnts) return fail(QBC_E_ARG, "qbc_build_tree: null points");
+  if (n == 0) pnts = reinterpret_cast<const float*>(&n);  // any non-null marker: no points to read
+  return build_into(c, tree, pnts, nullptr, n, basesize, levels, first_index, on_device);
+}
+
+extern "C" int qbc_build_tree_paths(qbc_ctx* c, int tree, const int32_t* octets, int64_t n, int levels,
+                                    int64_t first_index, int on_device) {
+  qbc::clear_error();
+  if (n > 0 && !octets) return fail(QBC_E_ARG, "qbc_build_tree_paths: null octets");
+  if (n == 0) octets = reinterpret_cast<const int32_t*>(&n);
+  return build_into(c, tree, nullptr, octets, n, 1.0f, levels, first_index, on_device);
+}
+
+extern "C" int qbc_download_tree(qbc_ctx* c, int tree, int32_t* nodes, int64_t cap, int64_t* n_nodes) {
+  qbc::clear_error();
+  if (!c || tree < 0 || tree > 1 || !n_nodes) return fail(QBC_E_ARG, "qbc_download_tree: bad argument");
+  const int64_t n = c->tree[tree].n;
+  *n_nodes = n;
+  if (!nodes || n == 0) return QBC_OK;
+  if (cap < n) return fail(QBC_E_ARG, "qbc_download_tree: capacity %lld below %lld nodes", (long long)cap, (long long)n);
+  QBC_CUDA(cudaSetDevice(c->device));
+  const int64_t chunk = (int64_t)(kStageMax / 48);
+  int rc = ensure_stage(c, (size_t)std::min(n, chunk) * 48);
+  if (rc) return rc;
+  for (int64_t a = 0; a < n; a += chunk) {
+    int64_t b = std::min(n, a + chunk);
+    unpack_nodes_kernel<<<launch_grid(c, b - a), 256, 0, c->stream>>>(c->tree[tree].child + 2 * a,
+                                                                       c->tree[tree].model + a, b - a,
+                                                                       (int4*)c->stage);
+    QBC_CUDA(cudaGetLastError());
+    ++c->launches;
+    QBC_CUDA(cudaMemcpyAsync(nodes + a * 12, c->stage, (size_t)(b - a) * 48, cudaMemcpyDeviceToHost, c->stream));
+  }
+  QBC_CUDA(cudaStreamSynchronize(c->stream));
+  return QBC_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Render
 // ---------------------------------------------------------------------------
 

@@ -165,6 +165,40 @@ class OctreeGLC:
     def set_stream(self, stream_ptr: Optional[int]) -> None:
         check(self._lib.qbc_set_stream(self.handle, C.c_void_p(stream_ptr or 0)))
 
+    def build_tree(self, dynamic: bool, points, basesize: float = 1800.0, levels: int = 12,
+                   first_index: int = 0) -> int:
+        """GPU build of the static or dynamic tree from points (numpy host
+        array, or a device pointer with `points=(ptr, n)`); returns the node count."""
+        if isinstance(points, tuple):
+            ptr, n, dev = int(points[0]), int(points[1]), 1
+        else:
+            p = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+            ptr, n, dev = p.ctypes.data, p.shape[0], 0
+        check(self._lib.qbc_build_tree(self.handle, 1 if dynamic else 0, C.c_void_p(ptr), n, float(basesize),
+                                       int(levels), int(first_index), dev))
+        return self.tree_nodes(1 if dynamic else 0)
+
+    def build_tree_paths(self, dynamic: bool, octets, levels: int = 12, first_index: int = 0) -> int:
+        if isinstance(octets, tuple):
+            ptr, n, dev = int(octets[0]), int(octets[1]), 1
+        else:
+            o = np.ascontiguousarray(octets, np.int32).reshape(-1, levels)
+            ptr, n, dev = o.ctypes.data, o.shape[0], 0
+        check(self._lib.qbc_build_tree_paths(self.handle, 1 if dynamic else 0, C.c_void_p(ptr), n, int(levels),
+                                             int(first_index), dev))
+        return self.tree_nodes(1 if dynamic else 0)
+
+    def download_tree(self, dynamic: bool) -> np.ndarray:
+        """The tree in the reference layout, shape (n, 12) int32."""
+        n = C.c_int64()
+        t = 1 if dynamic else 0
+        check(self._lib.qbc_download_tree(self.handle, t, None, 0, C.byref(n)))
+        out = np.zeros((n.value, 12), np.int32)
+        if n.value:
+            check(self._lib.qbc_download_tree(self.handle, t, out.ctypes.data_as(_lib.c_int32_p), n.value,
+                                              C.byref(n)))
+        return out
+
     def set_option(self, option: int, value: int) -> None:
         check(self._lib.qbc_set_option(self.handle, int(option), int(value)))
 
