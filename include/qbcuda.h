@@ -143,6 +143,26 @@ int qbc_destroy(qbc_ctx* ctx);
 int qbc_upload(qbc_ctx* ctx, const void* data, int type, size_t size, size_t itemsize, size_t start, size_t end, int buftype);
 
 /*
+ * qbc_upload with `data` in device memory of the context's GPU (for example
+ * the output of a skinning kernel), same argument meaning. Keeps the data on
+ * the device instead of a host round trip per frame (the reference reads the
+ * skinned paths back and re-uploads the dynamic tree and normals each frame,
+ * skeleton_glc.c:238-245, qubatron.c:508-529).
+ */
+int qbc_upload_device(qbc_ctx* ctx, const void* data, int type, size_t size, size_t itemsize, size_t start, size_t end, int buftype);
+
+/*
+ * Rigid skinning on the GPU: point i moves with bone[i], p' = R p + t and
+ * n' = R n, with bones[b] = {R row-major (9 floats), t (3 floats)}. Arrays
+ * are device memory; rest_nrms/out_nrms may both be NULL. A stand-in for the
+ * reference's skeleton shader (skeleton_vsh.c, gameplay) that drives the
+ * per-frame dynamic rebuild: skin, then qbc_build_tree(ctx, 1, out_pnts, ...,
+ * on_device = 1) and qbc_upload_device of the normals.
+ */
+#define QBC_MAX_BONES 64
+int qbc_skin_rigid(qbc_ctx* ctx, const float* rest_pnts, const float* rest_nrms, const int32_t* bone, int64_t n, const float* bones, int n_bones, float* out_pnts, float* out_nrms);
+
+/*
  * Derive the uniforms of one frame from the arguments of octree_glc_update
  * (octree_glc.c:249-284). focal <= 0 selects the reference's focal length
  * (ow/2)/tan(pi/4) (octree_fsh.c:403); a positive value sets cfp.z directly.

@@ -126,6 +126,10 @@ SIGNATURES = {
     "qbc_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
     "qbc_destroy": (C.c_int, [C.c_void_p]),
     "qbc_upload": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_size_t, C.c_size_t, C.c_size_t, C.c_size_t, C.c_int]),
+    "qbc_upload_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_size_t, C.c_size_t, C.c_size_t,
+                                    C.c_size_t, C.c_int]),
+    "qbc_skin_rigid": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, c_float_p, C.c_int,
+                                 C.c_void_p, C.c_void_p]),
     "qbc_view_setup": (C.c_int, [C.c_float, C.c_float, c_float_p, c_float_p, C.c_float, C.c_int, C.c_int,
                                  C.c_float, C.c_int, C.c_float, C.POINTER(View)]),
     "qbc_render": (C.c_int, [C.c_void_p, C.c_float, C.c_float, c_float_p, c_float_p, C.c_float, C.c_int, C.c_int,

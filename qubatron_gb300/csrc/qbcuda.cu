@@ -234,9 +234,26 @@ extern "C" int qbc_launch_count(qbc_ctx* c, int64_t* count) {
 // Upload (octree_glc_upload_texbuffer_data, octree_glc.c:361-498)
 // ---------------------------------------------------------------------------
 
+namespace {
+int upload_impl(qbc_ctx* c, const void* data, int type, size_t size, size_t itemsize, size_t start, size_t end,
+                int buftype, bool device_src);
+}
+
 extern "C" int qbc_upload(qbc_ctx* c, const void* data, int type, size_t size, size_t itemsize, size_t start,
                           size_t end, int buftype) {
   qbc::clear_error();
+  return upload_impl(c, data, type, size, itemsize, start, end, buftype, false);
+}
+
+extern "C" int qbc_upload_device(qbc_ctx* c, const void* data, int type, size_t size, size_t itemsize, size_t start,
+                                 size_t end, int buftype) {
+  qbc::clear_error();
+  return upload_impl(c, data, type, size, itemsize, start, end, buftype, true);
+}
+
+namespace {
+int upload_impl(qbc_ctx* c, const void* data, int type, size_t size, size_t itemsize, size_t start, size_t end,
+                int buftype, bool device_src) {
   if (!c) return fail(QBC_E_ARG, "qbc_upload: null context");
   if (buftype < QBC_STATIC_COLOR || buftype > QBC_DYNAMIC_OCTREE)
     return fail(QBC_E_ARG, "qbc_upload: unknown buffer %d", buftype);
@@ -270,16 +287,19 @@ extern "C" int qbc_upload(qbc_ctx* c, const void* data, int type, size_t size, s
     hi = std::min(hi, n_total);
     t.n = n_total;
     const int64_t chunk = (int64_t)(kStageMax / node_bytes);
-    if (hi > lo) {
+    if (hi > lo && !device_src) {
       int rc = ensure_stage(c, (size_t)std::min(hi - lo, chunk) * node_bytes);
       if (rc) return rc;
     }
     for (int64_t a = lo; a < hi; a += chunk) {
       int64_t b = std::min(hi, a + chunk);
-      QBC_CUDA(cudaMemcpyAsync(c->stage, base + a * node_bytes, (size_t)(b - a) * node_bytes, cudaMemcpyHostToDevice,
-                               c->stream));
+      const void* src = base + a * node_bytes;
+      if (!device_src) {
+        QBC_CUDA(cudaMemcpyAsync(c->stage, src, (size_t)(b - a) * node_bytes, cudaMemcpyHostToDevice, c->stream));
+        src = c->stage;
+      }
       qbc::repack_nodes_kernel<<<launch_grid(c, b - a), 256, 0, c->stream>>>(
-          (const int4*)c->stage, b - a, t.child + 2 * a, t.model + a);
+          (const int4*)src, b - a, t.child + 2 * a, t.model + a);
       QBC_CUDA(cudaGetLastError());
       ++c->launches;
     }
@@ -302,20 +322,90 @@ extern "C" int qbc_upload(qbc_ctx* c, const void* data, int type, size_t size, s
     }
     *n = n_total;
     const int64_t chunk = (int64_t)(kStageMax / 12);
-    if (hi > lo) {
+    if (hi > lo && !device_src) {
       int rc = ensure_stage(c, (size_t)std::min(hi - lo, chunk) * 12);
       if (rc) return rc;
     }
     for (int64_t a = lo; a < hi; a += chunk) {
       int64_t b = std::min(hi, a + chunk);
-      QBC_CUDA(cudaMemcpyAsync(c->stage, base + a * 12, (size_t)(b - a) * 12, cudaMemcpyHostToDevice, c->stream));
-      qbc::expand_attr_kernel<<<launch_grid(c, b - a), 256, 0, c->stream>>>((const float*)c->stage, b - a,
-                                                                             *arr + a, 1.0f);
+      const void* src = base + a * 12;
+      if (!device_src) {
+        QBC_CUDA(cudaMemcpyAsync(c->stage, src, (size_t)(b - a) * 12, cudaMemcpyHostToDevice, c->stream));
+        src = c->stage;
+      }
+      qbc::expand_attr_kernel<<<launch_grid(c, b - a), 256, 0, c->stream>>>((const float*)src, b - a, *arr + a,
+                                                                             1.0f);
       QBC_CUDA(cudaGetLastError());
       ++c->launches;
     }
   }
   QBC_CUDA(cudaStreamSynchronize(c->stream));
+  return QBC_OK;
+}
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Rigid skinning of a character for the dynamic tree
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct BoneSet {
+  float m[QBC_MAX_BONES][12];  // row-major 3x3 rotation, then translation
+};
+
+__global__ void skin_rigid_kernel(const float* __restrict__ rp, const float* __restrict__ rn,
+                                  const int32_t* __restrict__ bone, int64_t n, int n_bones,
+                                  const __grid_constant__ BoneSet bones, float* __restrict__ op,
+                                  float* __restrict__ on, int* __restrict__ bad) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int b = bone[i];
+    if (b < 0 || b >= n_bones) {
+      atomicExch(bad, 1);
+      b = 0;
+    }
+    const float* m = bones.m[b];
+    const float x = rp[3 * i], y = rp[3 * i + 1], z = rp[3 * i + 2];
+    op[3 * i] = m[0] * x + m[1] * y + m[2] * z + m[9];
+    op[3 * i + 1] = m[3] * x + m[4] * y + m[5] * z + m[10];
+    op[3 * i + 2] = m[6] * x + m[7] * y + m[8] * z + m[11];
+    if (rn && on) {
+      const float a = rn[3 * i], bb = rn[3 * i + 1], cc = rn[3 * i + 2];
+      on[3 * i] = m[0] * a + m[1] * bb + m[2] * cc;
+      on[3 * i + 1] = m[3] * a + m[4] * bb + m[5] * cc;
+      on[3 * i + 2] = m[6] * a + m[7] * bb + m[8] * cc;
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" int qbc_skin_rigid(qbc_ctx* c, const float* rest_pnts, const float* rest_nrms, const int32_t* bone,
+                              int64_t n, const float* bones, int n_bones, float* out_pnts, float* out_nrms) {
+  qbc::clear_error();
+  if (!c || (n > 0 && (!rest_pnts || !bone || !out_pnts)) || !bones)
+    return fail(QBC_E_ARG, "qbc_skin_rigid: null argument");
+  if (n_bones < 1 || n_bones > QBC_MAX_BONES)
+    return fail(QBC_E_ARG, "qbc_skin_rigid: %d bones outside 1..%d", n_bones, QBC_MAX_BONES);
+  if ((rest_nrms == nullptr) != (out_nrms == nullptr))
+    return fail(QBC_E_ARG, "qbc_skin_rigid: give both normal arrays or neither");
+  if (n == 0) return QBC_OK;
+  QBC_CUDA(cudaSetDevice(c->device));
+  BoneSet bs;
+  std::memset(&bs, 0, sizeof(bs));
+  std::memcpy(bs.m, bones, sizeof(float) * 12 * (size_t)n_bones);
+  int rc = ensure_stage(c, 256);
+  if (rc) return rc;
+  int* bad = (int*)c->stage;
+  QBC_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), c->stream));
+  skin_rigid_kernel<<<launch_grid(c, n), 256, 0, c->stream>>>(rest_pnts, rest_nrms, bone, n, n_bones, bs, out_pnts,
+                                                              out_nrms, bad);
+  QBC_CUDA(cudaGetLastError());
+  ++c->launches;
+  int hbad = 0;
+  QBC_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  QBC_CUDA(cudaStreamSynchronize(c->stream));
+  if (hbad) return fail(QBC_E_ARG, "qbc_skin_rigid: a bone index is outside 0..%d", n_bones - 1);
   return QBC_OK;
 }
 

@@ -199,6 +199,20 @@ class OctreeGLC:
                                               C.byref(n)))
         return out
 
+    def upload_device(self, ptr: int, type: int, size: int, itemsize: int, start: int, end: int,
+                      buftype: int) -> None:
+        """qbc_upload_device: the same upload from device memory at ptr."""
+        check(self._lib.qbc_upload_device(self.handle, C.c_void_p(int(ptr)), int(type), int(size), int(itemsize),
+                                          int(start), int(end), int(buftype)))
+
+    def skin_rigid(self, rest_pts: int, rest_nrm: int, bone: int, n: int, bones: np.ndarray, out_pts: int,
+                   out_nrm: int) -> None:
+        """qbc_skin_rigid on device pointers; bones is (n_bones, 12) float32."""
+        b = np.ascontiguousarray(bones, np.float32).reshape(-1, 12)
+        check(self._lib.qbc_skin_rigid(self.handle, C.c_void_p(rest_pts), C.c_void_p(rest_nrm), C.c_void_p(bone),
+                                       int(n), b.ctypes.data_as(_lib.c_float_p), b.shape[0], C.c_void_p(out_pts),
+                                       C.c_void_p(out_nrm)))
+
     def set_option(self, option: int, value: int) -> None:
         check(self._lib.qbc_set_option(self.handle, int(option), int(value)))
 

@@ -187,3 +187,118 @@ def workload_views(w: Workload, maxlevel: int = LEVELS, basesize: float = BASESI
     focal = vertical_fov_focal(w.height, w.fov_deg) if w.fov_deg else 0.0
     return [view_setup(w.width, w.height, pos, ang, w.lighta, w.quality, maxlevel, basesize, 0, focal)
             for pos, ang in w.poses]
+
+
+# ---------------------------------------------------------------------------
+# dynamic character: capsule limbs on a bone chain (the dynamic basecube)
+# ---------------------------------------------------------------------------
+
+@dataclass
+class Character:
+    rest_points: np.ndarray   # (n, 3) float32
+    rest_normals: np.ndarray  # (n, 3) float32
+    colors: np.ndarray        # (n, 3) float32
+    bone: np.ndarray          # (n,) int32, the bone each point moves with
+    joints: np.ndarray        # (n_bones + 1, 3) float64 rest joint positions
+
+
+def _unit_disc(rng, n):
+    """n unit vectors in the plane, by rejection (no trigonometry)."""
+    out = np.empty((0, 2))
+    while out.shape[0] < n:
+        u = rng.uniform(-1.0, 1.0, (2 * n, 2))
+        r2 = (u * u).sum(1)
+        u = u[(r2 > 1e-6) & (r2 <= 1.0)]
+        out = np.concatenate([out, u / np.sqrt((u * u).sum(1, keepdims=True))])
+    return out[:n]
+
+
+def _unit_sphere(rng, n):
+    out = np.empty((0, 3))
+    while out.shape[0] < n:
+        u = rng.uniform(-1.0, 1.0, (2 * n, 3))
+        r2 = (u * u).sum(1)
+        u = u[(r2 > 1e-6) & (r2 <= 1.0)]
+        out = np.concatenate([out, u / np.sqrt((u * u).sum(1, keepdims=True))])
+    return out[:n]
+
+
+def make_character(n_points: int, seed: int = 4, n_bones: int = 12, root=(900.0, 500.0, 1100.0),
+                   bone_len: float = 40.0, radius: float = 12.0) -> Character:
+    """A chain of n_bones capsules (radius, length bone_len) with seeded
+    zig-zag rest directions; points uniform on the capsule surfaces, exact
+    normals, one colour per limb."""
+    rng = np.random.default_rng(seed)
+    joints = [np.array(root, np.float64)]
+    for b in range(n_bones):
+        d = np.array([rng.uniform(-0.4, 0.4), 1.0, rng.uniform(-0.4, 0.4)])
+        joints.append(joints[-1] + bone_len * d / np.linalg.norm(d))
+    joints = np.array(joints)
+    cyl = 2.0 * np.pi * radius * bone_len
+    cap = 4.0 * np.pi * radius * radius
+    bone = rng.integers(0, n_bones, n_points).astype(np.int32)
+    on_cyl = rng.uniform(0.0, cyl + cap, n_points) < cyl
+    a = joints[bone]
+    axis = joints[bone + 1] - a
+    axis_n = axis / np.linalg.norm(axis, axis=1, keepdims=True)
+    # an orthonormal frame around each bone axis
+    helper = np.where(np.abs(axis_n[:, :1]) < 0.9, np.array([[1.0, 0.0, 0.0]]), np.array([[0.0, 1.0, 0.0]]))
+    e1 = np.cross(axis_n, helper)
+    e1 /= np.linalg.norm(e1, axis=1, keepdims=True)
+    e2 = np.cross(axis_n, e1)
+    disc = _unit_disc(rng, n_points)
+    radial = e1 * disc[:, :1] + e2 * disc[:, 1:]
+    t = rng.uniform(0.0, 1.0, (n_points, 1))
+    pts = a + axis * t + radius * radial
+    nrm = radial.copy()
+    sph = _unit_sphere(rng, n_points)
+    end = np.where((sph * axis_n).sum(1, keepdims=True) > 0.0, joints[bone + 1], a)
+    cap_pts = end + radius * sph
+    pts = np.where(on_cyl[:, None], pts, cap_pts)
+    nrm = np.where(on_cyl[:, None], nrm, sph)
+    limb_col = rng.uniform(0.2, 1.0, (n_bones, 3))
+    return Character(pts.astype(np.float32), nrm.astype(np.float32), limb_col[bone].astype(np.float32), bone,
+                     joints)
+
+
+def _rot(axis: int, ang: float) -> np.ndarray:
+    c, s = math.cos(ang), math.sin(ang)
+    if axis == 0:
+        return np.array([[1, 0, 0], [0, c, -s], [0, s, c]])
+    return np.array([[c, -s, 0], [s, c, 0], [0, 0, 1]])
+
+
+def pose_bones(ch: Character, frame: int, seed: int = 9, max_deg: float = 15.0) -> np.ndarray:
+    """Bone transforms of one frame: every bone turns by uniform +-max_deg
+    about its local x and z axes, accumulated down the chain (forward
+    kinematics). Returns (n_bones, 12) float32: row-major R, then t with
+    p' = R p + t."""
+    rng = np.random.default_rng([seed, frame])
+    n_bones = ch.joints.shape[0] - 1
+    out = np.zeros((n_bones, 12), np.float64)
+    R = np.eye(3)
+    j = ch.joints[0].copy()
+    lim = math.radians(max_deg)
+    for b in range(n_bones):
+        R = R @ _rot(0, rng.uniform(-lim, lim)) @ _rot(2, rng.uniform(-lim, lim))
+        t = j - R @ ch.joints[b]
+        out[b, :9] = R.reshape(-1)
+        out[b, 9:] = t
+        j = j + R @ (ch.joints[b + 1] - ch.joints[b])
+    return out.astype(np.float32)
+
+
+def skin_reference(ch: Character, bones: np.ndarray):
+    """Host skinning in float32 with the operation order of qbc_skin_rigid:
+    ((r0 x + r1 y) + r2 z) + t."""
+    m = bones[ch.bone]
+    p, n = ch.rest_points, ch.rest_normals
+    x, y, z = p[:, 0], p[:, 1], p[:, 2]
+    px = m[:, 0] * x + m[:, 1] * y + m[:, 2] * z + m[:, 9]
+    py = m[:, 3] * x + m[:, 4] * y + m[:, 5] * z + m[:, 10]
+    pz = m[:, 6] * x + m[:, 7] * y + m[:, 8] * z + m[:, 11]
+    a, b, c = n[:, 0], n[:, 1], n[:, 2]
+    nx = m[:, 0] * a + m[:, 1] * b + m[:, 2] * c
+    ny = m[:, 3] * a + m[:, 4] * b + m[:, 5] * c
+    nz = m[:, 6] * a + m[:, 7] * b + m[:, 8] * c
+    return np.stack([px, py, pz], 1).astype(np.float32), np.stack([nx, ny, nz], 1).astype(np.float32)

@@ -1,0 +1,68 @@
+"""The per-frame dynamic path on the GPU: rigid skinning of a character,
+rebuild of the dynamic tree from the skinned points, normals uploaded from
+device memory, and a frame rendered with both trees. Each frame is checked
+bit for bit: skinned points and normals against host float32 skinning in the
+same operation order, the dynamic tree against the CPU producer
+(octree_insert_point order), the frame against the oracle."""
+import numpy as np
+import pytest
+
+from conftest import LEVELS, S
+from helpers import compare_frame, gpu_frame, oracle_scene
+
+pytestmark = pytest.mark.gpu
+
+
+def test_character_frames(oracle, floor50k_scene):
+    torch = pytest.importorskip("torch")
+    import qubatron_gb300 as qb
+    from qubatron_gb300 import Octree, scenes, view_setup
+    s = floor50k_scene
+    ch = scenes.make_character(60000)
+    n = ch.rest_points.shape[0]
+    ctx = qb.OctreeGLC(0)
+    try:
+        ctx.upload_model(False, s.colors, s.normals)
+        ctx.upload_octree(False, s.nodes)
+        col = np.ascontiguousarray(ch.colors)
+        ctx.upload_texbuffer_data(col, qb.GL_FLOAT, col.nbytes, 12, 0, col.nbytes, qb.OCTREE_GLC_BUFFER_DYNAMIC_COLOR)
+        rp = torch.from_numpy(ch.rest_points).cuda()
+        rn = torch.from_numpy(ch.rest_normals).cuda()
+        bone = torch.from_numpy(ch.bone).cuda()
+        op = torch.empty_like(rp)
+        on = torch.empty_like(rn)
+        torch.cuda.synchronize()
+        v = view_setup(400, 300, (960.3, 700.2, 1700.7), (0.05, -0.2, 0.0), 0.4, 10, LEVELS, S, 0, 0.0)
+        for frame in range(3):
+            bones = scenes.pose_bones(ch, frame)
+            ctx.skin_rigid(rp.data_ptr(), rn.data_ptr(), bone.data_ptr(), n, bones, op.data_ptr(), on.data_ptr())
+            ctx.build_tree(True, (op.data_ptr(), n), S, LEVELS)
+            ctx.upload_device(on.data_ptr(), qb.GL_FLOAT, n * 12, 12, 0, n * 12, qb.OCTREE_GLC_BUFFER_DYNAMIC_NORMAL)
+            p_ref, n_ref = scenes.skin_reference(ch, bones)
+            np.testing.assert_array_equal(op.cpu().numpy().view(np.uint32), p_ref.view(np.uint32))
+            np.testing.assert_array_equal(on.cpu().numpy().view(np.uint32), n_ref.view(np.uint32))
+            t = Octree(S, LEVELS)
+            t.insert_points(p_ref)
+            d_nodes = t.nodes
+            np.testing.assert_array_equal(ctx.download_tree(True), d_nodes)
+            sc = oracle_scene(oracle, s.nodes, s.colors, s.normals, d_nodes, col, n_ref)
+            stats = compare_frame(gpu_frame(ctx, v), oracle.render(sc, oracle.QboView.from_bytes(v.to_bytes())),
+                                  f"character frame {frame}")
+            assert stats["primary_leaf"] > 500
+    finally:
+        ctx.close()
+
+
+def test_skin_rejects_bad_bone(floor50k_scene):
+    torch = pytest.importorskip("torch")
+    import qubatron_gb300 as qb
+    ctx = qb.OctreeGLC(0)
+    try:
+        p = torch.zeros((4, 3), dtype=torch.float32, device="cuda")
+        b = torch.tensor([0, 1, 5, 0], dtype=torch.int32, device="cuda")
+        o = torch.empty_like(p)
+        bones = np.zeros((2, 12), np.float32)
+        with pytest.raises(qb.QbcError):
+            ctx.skin_rigid(p.data_ptr(), 0, b.data_ptr(), 4, bones, o.data_ptr(), 0)
+    finally:
+        ctx.close()
