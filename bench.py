@@ -124,7 +124,40 @@ def prepare(workload_name: str):
     t = time.time()
     scene = scenes.make_scene(w.scene)
     views = scenes.workload_views(w)
-    return w, scene, views, time.time() - t
+    character = scenes.make_character(w.character) if w.character else None
+    return w, scene, views, character, time.time() - t
+
+
+class CharacterFrames:
+    """The dynamic basecube of a frame: skin the character on the GPU for the
+    frame's bone pose, rebuild the dynamic tree from the skinned points and
+    take the skinned normals, all on the device (qbc_skin_rigid,
+    qbc_build_tree, qbc_upload_device)."""
+
+    def __init__(self, ctx, ch):
+        import torch
+        import qubatron_gb300 as qb
+        self.qb, self.ctx, self.ch = qb, ctx, ch
+        self.n = ch.rest_points.shape[0]
+        self.rp = torch.from_numpy(ch.rest_points).cuda()
+        self.rn = torch.from_numpy(ch.rest_normals).cuda()
+        self.bone = torch.from_numpy(ch.bone).cuda()
+        self.op = torch.empty_like(self.rp)
+        self.on = torch.empty_like(self.rn)
+        col = np.ascontiguousarray(ch.colors)
+        ctx.upload_texbuffer_data(col, qb.GL_FLOAT, col.nbytes, 12, 0, col.nbytes, qb.OCTREE_GLC_BUFFER_DYNAMIC_COLOR)
+        torch.cuda.synchronize()
+
+    def bones(self, frame):
+        from qubatron_gb300 import scenes
+        return scenes.pose_bones(self.ch, frame)
+
+    def apply(self, bones):
+        qb, ctx, n = self.qb, self.ctx, self.n
+        ctx.skin_rigid(self.rp.data_ptr(), self.rn.data_ptr(), self.bone.data_ptr(), n, bones, self.op.data_ptr(),
+                       self.on.data_ptr())
+        ctx.build_tree(True, (self.op.data_ptr(), n), 1800.0, 12)
+        ctx.upload_device(self.on.data_ptr(), qb.GL_FLOAT, n * 12, 12, 0, n * 12, qb.OCTREE_GLC_BUFFER_DYNAMIC_NORMAL)
 
 
 def count_rays(flags: np.ndarray) -> int:
@@ -135,11 +168,18 @@ def count_rays(flags: np.ndarray) -> int:
     return primary + shadow + flare
 
 
-def cpu_sample(scene, views, budget_s: float, seed: int = 7):
-    """The oracle on a seeded pixel sample of the views, all host cores."""
+def cpu_sample(scene, views, budget_s: float, seed: int = 7, character=None, frame: int = 0):
+    """The oracle on a seeded pixel sample of the views, all host cores. With
+    a character, its pose of `frame` is skinned and built on the host."""
     from oracle import qbo
     threads = os.cpu_count() or 1
-    sc = qbo.Scene(scene.nodes, scene.colors, scene.normals)
+    if character is not None:
+        from qubatron_gb300 import scenes
+        from qubatron_gb300.octree import build_octree
+        p, n = scenes.skin_reference(character, scenes.pose_bones(character, frame))
+        sc = qbo.Scene(scene.nodes, scene.colors, scene.normals, build_octree(p), character.colors, n)
+    else:
+        sc = qbo.Scene(scene.nodes, scene.colors, scene.normals)
     ov = [qbo.QboView.from_bytes(v.to_bytes()) for v in views]
     rng = np.random.default_rng(seed)
 
@@ -152,12 +192,19 @@ def cpu_sample(scene, views, budget_s: float, seed: int = 7):
             rays += count_rays(out["flags"])
         return rays, time.perf_counter() - t0
 
-    rays, dt = run(256)  # calibration
-    rate = rays / max(dt, 1e-6)
-    per_view = int(max(256, min(200000, budget_s * rate / (len(ov) * 2.05))))
-    rays, dt = run(per_view)
+    # time-boxed: batches of seeded pixels of every view until the budget is spent
+    run(64)  # warm the caches and the thread pool
+    rays, dt, per_view, rounds = 0, 0.0, 2048, 0
+    while dt < budget_s:
+        r, t = run(per_view)
+        rays += r
+        dt += t
+        rounds += 1
+        if t < budget_s / 8:
+            per_view *= 2
     return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
-            "sample": f"{per_view} seeded pixels x {len(ov)} views of the same workload ({rays} rays, {dt:.1f} s)",
+            "sample": f"{rounds} rounds of seeded pixels over all {len(ov)} views of the same workload "
+                      f"({rays} rays, {dt:.1f} s)",
             "seconds": dt, "rays": rays}
 
 
@@ -165,13 +212,15 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    w, scene, views, _ = prepare(WORKLOAD)
+    w, scene, views, character, _ = prepare(WORKLOAD)
     # each step: a bounded sample (~8 s) of the workload's pixels
     from oracle import qbo  # noqa: F401
     times, rays_total = [], 0
     res = None
     for step in range(args.warmup + args.steps):
-        res = cpu_sample(scene, views, budget_s=8.0, seed=100 + step)
+        # per step a bounded sample: 6 s of CPU work at most, warm-up steps 2 s
+        budget = min(args.cpu_seconds, 6.0) if step >= args.warmup else 2.0
+        res = cpu_sample(scene, views, budget_s=budget, seed=100 + step, character=character, frame=step)
         if step >= args.warmup:
             times.append(res["seconds"])
             rays_total += res["rays"]
@@ -192,7 +241,7 @@ def run_reference(args):
     return 0
 
 
-def measure_e2e(ctx, views, rays, world, flush, steps):
+def measure_e2e(ctx, views, rays, world, flush, steps, update=None):
     """Same views through the public C ABI into pinned host buffers: the
     timed call includes the kernel and the copy of every frame to the host."""
     import torch
@@ -206,10 +255,12 @@ def measure_e2e(ctx, views, rays, world, flush, steps):
     for _ in range(2):
         ctx.render_views(views, houts, on_device=False)
     e2e_t = []
-    for _ in range(max(3, steps)):
+    for k in range(max(3, steps)):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        if update:
+            update(k)
         ctx.render_views(views, houts, on_device=False)
         e2e_t.append(time.perf_counter() - t0)
     e2e_s = statistics.mean(e2e_t)
@@ -228,7 +279,7 @@ def run_gpu(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    w, scene, views, prep_s = prepare(WORKLOAD)
+    w, scene, views, character, prep_s = prepare(WORKLOAD)
 
     ctx = qb.OctreeGLC(local)
     # a dedicated stream: the library and the timing events must share it
@@ -250,35 +301,49 @@ def run_gpu(args):
         o.rgba8 = f.data_ptr()
         outs.append(o)
 
-    # one untimed instrumented pass: rays cast and node visits per step
+    chars = CharacterFrames(ctx, character) if character is not None else None
+    n_frames = args.warmup + args.steps
+    poses = [chars.bones(f) for f in range(n_frames)] if chars else [None] * n_frames
+
+    def update(frame):
+        if chars:
+            chars.apply(poses[frame])
+
+    # untimed instrumented passes: rays cast and node visits of every timed
+    # frame (a static scene needs one)
     flags = [torch.empty((v.height_px, v.width_px), dtype=torch.int32, device="cuda") for v in views]
     visits = [torch.empty((v.height_px, v.width_px, 4), dtype=torch.int32, device="cuda") for v in views]
-    isp = [torch.empty((v.height_px, v.width_px, 4), dtype=torch.float32, device="cuda") for v in views]
     inst = []
-    for f, fl, vi, ip in zip(frames, flags, visits, isp):
+    for f, fl, vi in zip(frames, flags, visits):
         o = qb.Outputs()
         o.rgba8 = f.data_ptr()
         o.flags = fl.data_ptr()
         o.visits = vi.data_ptr()
-        o.leaf = 0
-        o.isp = ip.data_ptr()
         inst.append(o)
-    ctx.render_views(views, inst, on_device=True)
-    torch.cuda.synchronize()
-    rays = 0
-    vis_total = 0
-    leaves = 0
-    for fl, vi in zip(flags, visits):
-        f = fl.cpu().numpy().view(np.uint32)
-        rays += count_rays(f)
-        leaves += int((f & 1).sum()) + int(((f >> 3) & 1).sum())
-        vis_total += int(vi.to(torch.int64).sum().item())
-    pixels = sum(v.width_px * v.height_px for v in views)
-    alg_bytes = vis_total * BYTES_PER_VISIT + leaves * BYTES_PER_LEAF + pixels * BYTES_PER_PIXEL_OUT
-    del flags, visits, isp
+    frame_rays, frame_bytes = [], []
+    for k in range(args.steps if chars else 1):
+        update(args.warmup + k)
+        ctx.render_views(views, inst, on_device=True)
+        torch.cuda.synchronize()
+        rays_k, vis_k, leaves_k = 0, 0, 0
+        for fl, vi in zip(flags, visits):
+            f = fl.cpu().numpy().view(np.uint32)
+            rays_k += count_rays(f)
+            leaves_k += int((f & 1).sum()) + int(((f >> 3) & 1).sum())
+            vis_k += int(vi.to(torch.int64).sum().item())
+        pixels = sum(v.width_px * v.height_px for v in views)
+        frame_rays.append(rays_k)
+        frame_bytes.append(vis_k * BYTES_PER_VISIT + leaves_k * BYTES_PER_LEAF + pixels * BYTES_PER_PIXEL_OUT)
+    if not chars:
+        frame_rays *= args.steps
+        frame_bytes *= args.steps
+    rays = statistics.mean(frame_rays)
+    alg_bytes = statistics.mean(frame_bytes)
+    del flags, visits
 
     flush = torch.empty(2 * L2_BYTES, dtype=torch.uint8, device="cuda")
-    for _ in range(args.warmup):
+    for f in range(args.warmup):
+        update(f)
         ctx.render_views(views, outs, on_device=True)
     torch.cuda.synchronize()
 
@@ -291,6 +356,7 @@ def run_gpu(args):
         for k in range(args.steps):
             flush.zero_()
             ev[k][0].record(stream)
+            update(args.warmup + k)
             ctx.render_views(views, outs, on_device=True)
             ev[k][1].record(stream)
         torch.cuda.synchronize()
@@ -303,11 +369,23 @@ def run_gpu(args):
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
-    value = world * rays / (ms / 1000.0) / 1e6
+    value = world * sum(frame_rays) / (sum(step_ms) / 1000.0) / 1e6
+
+    update_ms = None
+    if chars:
+        # the dynamic-tree update alone (skin + rebuild + normals), untimed above
+        ue = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(3)]
+        for k in range(3):
+            ue[k][0].record(stream)
+            update(args.warmup + k % args.steps)
+            ue[k][1].record(stream)
+        torch.cuda.synchronize()
+        update_ms = statistics.mean(a.elapsed_time(b) for a, b in ue)
 
     e2e = None
     if not args.no_e2e:
-        e2e = measure_e2e(ctx, views, rays, world, flush, args.steps)
+        e2e = measure_e2e(ctx, views, rays, world, flush, args.steps,
+                          (lambda k: update(args.warmup + k % args.steps)) if chars else None)
 
     hbm, peak_kind = peaks()
 
@@ -325,8 +403,11 @@ def run_gpu(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
         "config": {"workload": WORKLOAD, "points": int(scene.points.shape[0]), "nodes": int(scene.nodes.shape[0]),
-                   "resolution": f"{w.width}x{w.height}", "views": len(views), "depth": 12, "basecube": 1800.0,
-                   "rays_per_step": rays, "nominal_2wh_rays_per_step": 2 * pixels,
+                   "resolution": f"{w.width}x{w.height}" if w.width else "mixed", "views": len(views), "depth": 12,
+                   "basecube": 1800.0, "rays_per_step": rays, "nominal_2wh_rays_per_step": 2 * pixels,
+                   "dynamic_points": int(w.character),
+                   "per_step": "re-skin + rebuild dynamic tree + render" if chars else "render",
+                   "dynamic_update_ms": update_ms,
                    "l2": "flushed between steps (2x L2 write, outside the timed events); node arrays "
                          f"{scene.nodes.shape[0] * 36 / 1e9:.2f} GB > L2",
                    "parallelism": "replicas only" if world > 1 else "single GPU",
@@ -340,7 +421,8 @@ def run_gpu(args):
         "step_ms": [round(x, 4) for x in step_ms],
     }
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = {k: v for k, v in cpu_sample(scene, views, budget_s=args.cpu_seconds).items()
+        line["cpu_baseline"] = {k: v for k, v in cpu_sample(scene, views, budget_s=args.cpu_seconds,
+                                                            character=character, frame=args.warmup).items()
                                 if k not in ("seconds", "rays")}
     ctx.close()
     if rank == 0:

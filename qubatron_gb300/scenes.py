@@ -171,6 +171,31 @@ class Workload:
     lighta: float = 0.0
     quality: int = 10
     fov_deg: float = 60.0
+    sizes: List = None        # per-view (width, height) when views differ in size
+    character: int = 0        # points of a dynamic character re-skinned every frame
+
+
+def aim(pos, target):
+    """(yaw, pitch) that point the camera of octree_fsh.c:406-413 from pos at
+    target: the unrotated ray looks down -z, yaw turns it towards +x, pitch up."""
+    dx, dy, dz = (target[i] - pos[i] for i in range(3))
+    return (float(np.float32(math.atan2(dx, -dz))), float(np.float32(math.atan2(dy, math.hypot(dx, dz)))), 0.0)
+
+
+def batch_views(seed: int, n: int, target=(960.0, 700.0, 1150.0)):
+    """n views with sizes drawn uniformly from {320x240, 640x480, 1280x720,
+    1920x1080, 3840x2160}, cameras on a seeded ring around target."""
+    rng = _SplitMix(seed)
+    choices = [(320, 240), (640, 480), (1280, 720), (1920, 1080), (3840, 2160)]
+    sizes, poses = [], []
+    for _ in range(n):
+        sizes.append(choices[min(4, int(rng.uniform(0.0, 5.0)))])
+        ang = rng.uniform(0.0, 2.0 * math.pi)
+        r = rng.uniform(450.0, 750.0)
+        pos = (float(np.float32(target[0] + r * math.sin(ang))), float(np.float32(rng.uniform(250.0, 1000.0))),
+               float(np.float32(target[2] + r * math.cos(ang))))
+        poses.append((pos, aim(pos, target)))
+    return sizes, poses
 
 
 WORKLOADS = {
@@ -178,15 +203,19 @@ WORKLOADS = {
     "room20m_1920x1080x16": Workload("room20m_1920x1080x16", "room20m", 1920, 1080, spline_poses(1002, 16)),
     "room5m_1920x1080x1": Workload("room5m_1920x1080x1", "room5m", 1920, 1080, spline_poses(1002, 16)[:1]),
 }
+_b64_sizes, _b64_poses = batch_views(64, 64)
+WORKLOADS["floor1m_char2m_mixed_x64"] = Workload("floor1m_char2m_mixed_x64", "floor1m", 0, 0, _b64_poses,
+                                                 sizes=_b64_sizes, character=2_000_000)
 
 
 def workload_views(w: Workload, maxlevel: int = LEVELS, basesize: float = BASESIZE):
     """qbc_view per pose: the reference's uniforms with the configured
     vertical field of view."""
     from .octree_glc import view_setup
-    focal = vertical_fov_focal(w.height, w.fov_deg) if w.fov_deg else 0.0
-    return [view_setup(w.width, w.height, pos, ang, w.lighta, w.quality, maxlevel, basesize, 0, focal)
-            for pos, ang in w.poses]
+    sizes = w.sizes or [(w.width, w.height)] * len(w.poses)
+    return [view_setup(sw, sh, pos, ang, w.lighta, w.quality, maxlevel, basesize, 0,
+                       vertical_fov_focal(sh, w.fov_deg) if w.fov_deg else 0.0)
+            for (sw, sh), (pos, ang) in zip(sizes, w.poses)]
 
 
 # ---------------------------------------------------------------------------
