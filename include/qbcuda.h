@@ -240,6 +240,56 @@ int qbc_trace_rays(qbc_ctx* ctx, const float* pos, const float* dir, int64_t n, 
 #define QBC_NOALLOC_MAX_VIEWS (QBC_NOALLOC_MAX_LAUNCHES * 32)
 int qbc_render_views_noalloc(qbc_ctx* ctx, const qbc_view* views, const qbc_outputs* outs, int n);
 
+/*
+ * Options of qbc_render_views_ex.
+ *   two_pass        0: one fused kernel (as qbc_render_views). 1: a primary
+ *                   pass that queues the shaded and flare pixels (compacted
+ *                   with warp-aggregated atomics), then a shade pass over the
+ *                   queue: shadow ray, shading, flare.
+ *   proposals       (two_pass only) cells to test before the plain shadow
+ *                   walk: QBC_PROPOSE_NONE, QBC_PROPOSE_MLP (the occluder
+ *                   network of qbc_proposal_*), QBC_PROPOSE_LOGGED (the first
+ *                   leaf a previous logged render of the same views found),
+ *                   QBC_PROPOSE_RANDOM (seeded, for tests).
+ *   log             (two_pass only) record, per queued pixel, the t of the
+ *                   plain shadow walk's first leaf and its lit bit.
+ *   proposal_level  level of the proposed cells (default 8 when 0).
+ *   seed            QBC_PROPOSE_RANDOM seed.
+ * A proposal is a point on the shadow ray; its level-`proposal_level` cell is
+ * entered exactly as the plain walk would enter it (same candidates, same
+ * entry point) and only its subtree is walked. A leaf found there more than
+ * 4 units before the primary hit proves the pixel unlit: the plain walk's
+ * first leaf is at least as early along the ray. Otherwise the plain walk
+ * runs. Every pixel's colour, flags, primary leaf and intersection are thus
+ * identical to the plain result; for proven pixels the shadow-leaf output is
+ * -2 (not computed) and the shadow visit counts are the proposal walks'.
+ */
+#define QBC_PROPOSE_NONE 0
+#define QBC_PROPOSE_MLP 1
+#define QBC_PROPOSE_LOGGED 2
+#define QBC_PROPOSE_RANDOM 3
+typedef struct qbc_render_opts
+{
+    int32_t  two_pass;
+    int32_t  proposals;
+    int32_t  log;
+    int32_t  proposal_level;
+    uint64_t seed;
+} qbc_render_opts;
+
+/* Counters of the last qbc_render_views_ex call (two_pass only). */
+typedef struct qbc_render_stats
+{
+    uint64_t queued;            /* pixels in the shade pass */
+    uint64_t shadow_rays;       /* plain shadow walks */
+    uint64_t shadow_visits;     /* node visits of plain shadow walks */
+    uint64_t proposals_tried;   /* proposal walks */
+    uint64_t proposals_proven;  /* shadow rays settled by a proposal */
+    uint64_t proposal_visits;   /* node visits of proposal walks */
+} qbc_render_stats;
+
+int qbc_render_views_ex(qbc_ctx* ctx, const qbc_view* views, const qbc_outputs* outs, int n, int outputs_on_device, const qbc_render_opts* opts, qbc_render_stats* stats);
+
 /* Run the context's work on this CUDA stream (a cudaStream_t; NULL = the
  * context's own stream). */
 int qbc_set_stream(qbc_ctx* ctx, void* stream);

@@ -100,6 +100,37 @@ class RayHits(C.Structure):
     ]
 
 
+class RenderOpts(C.Structure):
+    """qbc_render_opts."""
+
+    _fields_ = [
+        ("two_pass", C.c_int32),
+        ("proposals", C.c_int32),
+        ("log", C.c_int32),
+        ("proposal_level", C.c_int32),
+        ("seed", C.c_uint64),
+    ]
+
+
+class RenderStats(C.Structure):
+    """qbc_render_stats."""
+
+    _fields_ = [
+        ("queued", C.c_uint64),
+        ("shadow_rays", C.c_uint64),
+        ("shadow_visits", C.c_uint64),
+        ("proposals_tried", C.c_uint64),
+        ("proposals_proven", C.c_uint64),
+        ("proposal_visits", C.c_uint64),
+    ]
+
+    def as_dict(self) -> dict:
+        return {f: int(getattr(self, f)) for f, _ in self._fields_}
+
+
+PROPOSE_NONE, PROPOSE_MLP, PROPOSE_LOGGED, PROPOSE_RANDOM = 0, 1, 2, 3
+
+
 class SceneDesc(C.Structure):
     """qbc_scene_desc."""
 
@@ -137,6 +168,8 @@ SIGNATURES = {
     "qbc_render_views": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int, C.c_int]),
     "qbc_trace_rays": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, c_float_p, C.c_int,
                                  C.POINTER(RayHits), C.c_int]),
+    "qbc_render_views_ex": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int, C.c_int,
+                                      C.POINTER(RenderOpts), C.POINTER(RenderStats)]),
     "qbc_render_views_noalloc": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int]),
     "qbc_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "qbc_synchronize": (C.c_int, [C.c_void_p]),

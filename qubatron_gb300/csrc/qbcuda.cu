@@ -69,6 +69,14 @@ struct qbc_ctx {
   void* scratch = nullptr;  // device outputs for host-output renders
   size_t scratch_bytes = 0;
   unsigned int* queue = nullptr;  // global tile counter of the persistent render kernel
+  // two-pass render: records, counters (queued, shade-pass next), statistics, per-pixel log
+  uint32_t* rec = nullptr;
+  int64_t rec_cap = 0;
+  unsigned int* wcount = nullptr;
+  unsigned long long* wstats = nullptr;
+  float* pixlog = nullptr;
+  int64_t pixlog_cap = 0;
+  int64_t pixlog_valid = 0;  // pixels of the last logged render (0: none)
   int render_blocks[4] = {0, 0, 0, 0};  // resident blocks per SM of each render_kernel variant
   int attr_done = 0;
   int service_min = qbc::kServiceMinDefault;
@@ -153,6 +161,8 @@ extern "C" int qbc_create(int device, qbc_ctx** out) {
     return cuda_fail(e, "qbc_create");
   }
   if (e == cudaSuccess) e = cudaMalloc(&c->queue, sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMalloc(&c->wcount, 2 * sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMalloc(&c->wstats, qbc::kStatCount * sizeof(unsigned long long));
   if (e != cudaSuccess) {
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
@@ -176,6 +186,10 @@ extern "C" int qbc_destroy(qbc_ctx* c) {
   cudaFree(c->stage);
   cudaFree(c->scratch);
   cudaFree(c->queue);
+  cudaFree(c->rec);
+  cudaFree(c->wcount);
+  cudaFree(c->wstats);
+  cudaFree(c->pixlog);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return QBC_OK;
@@ -542,10 +556,33 @@ void** out_slot(qbc_outputs& o, int k) {
   }
 }
 
-template <bool EXACT, bool DYN>
-int launch_render(qbc_ctx* c, const qbc::Batch& b, size_t smem) {
-  auto kern = qbc::render_kernel<EXACT, DYN>;
-  const int variant = (EXACT ? 1 : 0) + (DYN ? 2 : 0);
+int propose_mlp(qbc_ctx* c, const qbc::Wave& w) {
+  (void)w;
+  (void)c;
+  return fail(QBC_E_STATE, "qbc_render_views_ex: no occluder network trained in this context");
+}
+
+// Statistics of the shade passes of the last two-pass render (synchronizes).
+int read_stats(qbc_ctx* c, qbc_render_stats* stats) {
+  if (!stats) return QBC_OK;
+  unsigned long long h[qbc::kStatCount];
+  unsigned int q[2];
+  QBC_CUDA(cudaMemcpyAsync(h, c->wstats, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  QBC_CUDA(cudaMemcpyAsync(q, c->wcount, sizeof(q), cudaMemcpyDeviceToHost, c->stream));
+  QBC_CUDA(cudaStreamSynchronize(c->stream));
+  stats->queued = q[0];
+  stats->shadow_rays = h[qbc::kStatShadowRays];
+  stats->shadow_visits = h[qbc::kStatShadowVisits];
+  stats->proposals_tried = h[qbc::kStatPropTried];
+  stats->proposals_proven = h[qbc::kStatPropProven];
+  stats->proposal_visits = h[qbc::kStatPropVisits];
+  return QBC_OK;
+}
+
+template <bool EXACT, bool DYN, int MODE, bool PROP>
+int launch_render(qbc_ctx* c, const qbc::Batch& b, size_t smem, const qbc::Wave& wave) {
+  auto kern = qbc::render_kernel<EXACT, DYN, MODE, PROP>;
+  const int variant = (EXACT ? 1 : 0) + (DYN ? 2 : 0) + 4 * MODE + (PROP ? 16 : 0);
   if (!(c->attr_done & (1 << variant))) {
     QBC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
     c->attr_done |= 1 << variant;
@@ -553,20 +590,72 @@ int launch_render(qbc_ctx* c, const qbc::Batch& b, size_t smem) {
   int per_sm = 0;
   QBC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, qbc::kThreads, smem));
   if (per_sm < 1) return fail(QBC_E_STATE, "render_kernel: no block fits on an SM with %zu B shared memory", smem);
-  c->render_blocks[variant] = per_sm;
+  if (MODE == qbc::kFused && !PROP) c->render_blocks[(EXACT ? 1 : 0) + (DYN ? 2 : 0)] = per_sm;
   // persistent: one wave of resident blocks, never more blocks than warp tiles
-  int64_t blocks = std::min<int64_t>((int64_t)per_sm * c->sm_count, ((int64_t)b.tiles_total + 3) / 4);
+  int64_t blocks = (int64_t)per_sm * c->sm_count;
+  if (MODE != qbc::kShadePass) blocks = std::min<int64_t>(blocks, ((int64_t)b.tiles_total + 3) / 4);
   blocks = std::max<int64_t>(blocks, 1);
-  QBC_CUDA(cudaMemsetAsync(c->queue, 0, sizeof(unsigned int), c->stream));
-  kern<<<(unsigned)blocks, qbc::kThreads, smem, c->stream>>>(device_scene(c), b, c->queue);
+  if (MODE != qbc::kShadePass) QBC_CUDA(cudaMemsetAsync(c->queue, 0, sizeof(unsigned int), c->stream));
+  kern<<<(unsigned)blocks, qbc::kThreads, smem, c->stream>>>(device_scene(c), b, c->queue, wave);
   QBC_CUDA(cudaGetLastError());
   ++c->launches;
   return QBC_OK;
 }
 
-int launch_batch(qbc_ctx* c, const qbc_view* views, const qbc_outputs* dev_outs, int n) {
+template <bool EXACT, bool DYN>
+int launch_modes(qbc_ctx* c, const qbc::Batch& b, size_t smem, const qbc_render_opts* opts, int64_t pixels) {
+  if (!opts || !opts->two_pass) return launch_render<EXACT, DYN, qbc::kFused, false>(c, b, smem, qbc::Wave{});
+  // two passes: primary rays -> record queue -> shade pass
+  if (c->rec_cap < pixels) {
+    int rc = grow(&c->rec, &c->rec_cap, pixels, (size_t)qbc::kRecWords * 4, "render records");
+    if (rc) return rc;
+  }
+  const bool want_log = opts->log || opts->proposals == QBC_PROPOSE_LOGGED;
+  if (want_log && c->pixlog_cap < pixels) {
+    int rc = grow(&c->pixlog, &c->pixlog_cap, pixels, 4, "render log");
+    if (rc) return rc;
+  }
+  if (opts->proposals == QBC_PROPOSE_LOGGED && c->pixlog_valid != pixels)
+    return fail(QBC_E_STATE, "qbc_render_views_ex: logged proposals need a logged render of the same views first");
+  qbc::Wave w{};
+  w.rec = c->rec;
+  w.qcount = c->wcount;
+  w.qnext = c->wcount + 1;
+  w.stats = c->wstats;
+  w.cap = (uint32_t)std::min<int64_t>(c->rec_cap, 0xFFFFFFFFll);
+  w.log = opts->log ? 1 : 0;
+  w.nprop = opts->proposals != QBC_PROPOSE_NONE ? 3 : 0;
+  w.pdepth = opts->proposal_level > 0 ? opts->proposal_level : 8;
+  w.pixlog = opts->log ? c->pixlog : nullptr;
+  QBC_CUDA(cudaMemsetAsync(c->wcount, 0, 2 * sizeof(unsigned int), c->stream));
+  int rc = launch_render<EXACT, DYN, qbc::kPrimaryPass, false>(c, b, smem, w);
+  if (rc) return rc;
+  if (opts->proposals == QBC_PROPOSE_LOGGED) {
+    qbc::Wave lw = w;
+    lw.pixlog = c->pixlog;
+    qbc::fill_logged_proposals<<<c->sm_count * 8, 256, 0, c->stream>>>(b, lw);
+    QBC_CUDA(cudaGetLastError());
+    ++c->launches;
+  } else if (opts->proposals == QBC_PROPOSE_RANDOM) {
+    qbc::fill_random_proposals<<<c->sm_count * 8, 256, 0, c->stream>>>(w, (unsigned long long)opts->seed);
+    QBC_CUDA(cudaGetLastError());
+    ++c->launches;
+  } else if (opts->proposals == QBC_PROPOSE_MLP) {
+    rc = propose_mlp(c, w);
+    if (rc) return rc;
+  }
+  if (w.nprop > 0) rc = launch_render<EXACT, DYN, qbc::kShadePass, true>(c, b, smem, w);
+  else rc = launch_render<EXACT, DYN, qbc::kShadePass, false>(c, b, smem, w);
+  if (rc) return rc;
+  if (opts->log) c->pixlog_valid = pixels;
+  return QBC_OK;
+}
+
+int launch_batch(qbc_ctx* c, const qbc_view* views, const qbc_outputs* dev_outs, int n,
+                 const qbc_render_opts* opts = nullptr) {
   qbc::Batch* b = new qbc::Batch();
   int tiles = 0, maxlevel = 0;
+  int64_t pixels = 0;
   bool exact = true;
   for (int i = 0; i < n; ++i) {
     qbc::ViewJob& J = b->job[i];
@@ -575,7 +664,9 @@ int launch_batch(qbc_ctx* c, const qbc_view* views, const qbc_outputs* dev_outs,
     J.tiles_x = (views[i].width_px + 7) / 8;
     int tiles_y = (views[i].height_px + 3) / 4;
     J.tile_begin = tiles;
+    J.pixel_begin = pixels;
     tiles += J.tiles_x * tiles_y;
+    pixels += (int64_t)views[i].width_px * views[i].height_px;
     maxlevel = std::max(maxlevel, views[i].maxlevel);
     exact = exact && qbc::cube_shift_exact(views[i]);
   }
@@ -588,18 +679,43 @@ int launch_batch(qbc_ctx* c, const qbc_view* views, const qbc_outputs* dev_outs,
   const size_t smem = words * qbc::kThreads * sizeof(uint32_t);
   int rc;
   if (exact)
-    rc = dyn ? launch_render<true, true>(c, *b, smem) : launch_render<true, false>(c, *b, smem);
+    rc = dyn ? launch_modes<true, true>(c, *b, smem, opts, pixels) : launch_modes<true, false>(c, *b, smem, opts, pixels);
   else
-    rc = dyn ? launch_render<false, true>(c, *b, smem) : launch_render<false, false>(c, *b, smem);
+    rc = dyn ? launch_modes<false, true>(c, *b, smem, opts, pixels) : launch_modes<false, false>(c, *b, smem, opts, pixels);
   delete b;
   return rc;
 }
 
 }  // namespace
 
+namespace {
+int render_views_impl(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs, int n, int outputs_on_device,
+                      const qbc_render_opts* opts, qbc_render_stats* stats);
+}
+
 extern "C" int qbc_render_views(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs, int n,
                                 int outputs_on_device) {
   qbc::clear_error();
+  return render_views_impl(c, views, outs, n, outputs_on_device, nullptr, nullptr);
+}
+
+extern "C" int qbc_render_views_ex(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs, int n,
+                                   int outputs_on_device, const qbc_render_opts* opts, qbc_render_stats* stats) {
+  qbc::clear_error();
+  if (opts && (opts->proposals < QBC_PROPOSE_NONE || opts->proposals > QBC_PROPOSE_RANDOM))
+    return fail(QBC_E_ARG, "qbc_render_views_ex: unknown proposal source %d", opts->proposals);
+  if (opts && opts->proposals != QBC_PROPOSE_NONE && !opts->two_pass)
+    return fail(QBC_E_ARG, "qbc_render_views_ex: proposals need two_pass");
+  if (opts && (opts->proposal_level < 0 || opts->proposal_level > QBC_MAX_LEVEL))
+    return fail(QBC_E_ARG, "qbc_render_views_ex: proposal_level %d outside 0..%d", opts->proposal_level, QBC_MAX_LEVEL);
+  if (opts && opts->two_pass && n > qbc::kMaxViewsPerLaunch)
+    return fail(QBC_E_ARG, "qbc_render_views_ex: two-pass renders take at most %d views per call", qbc::kMaxViewsPerLaunch);
+  return render_views_impl(c, views, outs, n, outputs_on_device, opts, stats);
+}
+
+namespace {
+int render_views_impl(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs, int n, int outputs_on_device,
+                      const qbc_render_opts* opts, qbc_render_stats* stats) {
   if (!c || (n > 0 && (!views || !outs))) return fail(QBC_E_ARG, "qbc_render_views: null argument");
   if (n < 0) return fail(QBC_E_ARG, "qbc_render_views: negative view count");
   QBC_CUDA(cudaSetDevice(c->device));
@@ -608,12 +724,14 @@ extern "C" int qbc_render_views(qbc_ctx* c, const qbc_view* views, const qbc_out
     if (rc) return rc;
   }
 
+  const bool two = opts && opts->two_pass;
+  if (two) QBC_CUDA(cudaMemsetAsync(c->wstats, 0, qbc::kStatCount * sizeof(unsigned long long), c->stream));
   if (outputs_on_device) {
     for (int a = 0; a < n; a += qbc::kMaxViewsPerLaunch) {
-      int rc = launch_batch(c, views + a, outs + a, std::min(qbc::kMaxViewsPerLaunch, n - a));
+      int rc = launch_batch(c, views + a, outs + a, std::min(qbc::kMaxViewsPerLaunch, n - a), opts);
       if (rc) return rc;
     }
-    return QBC_OK;
+    return two ? read_stats(c, stats) : QBC_OK;
   }
 
   // host outputs: render into device scratch, then copy each stream back
@@ -645,7 +763,7 @@ extern "C" int qbc_render_views(qbc_ctx* c, const qbc_view* views, const qbc_out
     }
   }
   for (int a = 0; a < n; a += qbc::kMaxViewsPerLaunch) {
-    int rc = launch_batch(c, views + a, dev.data() + a, std::min(qbc::kMaxViewsPerLaunch, n - a));
+    int rc = launch_batch(c, views + a, dev.data() + a, std::min(qbc::kMaxViewsPerLaunch, n - a), opts);
     if (rc) return rc;
   }
   for (int i = 0; i < n; ++i) {
@@ -658,8 +776,9 @@ extern "C" int qbc_render_views(qbc_ctx* c, const qbc_view* views, const qbc_out
     }
   }
   QBC_CUDA(cudaStreamSynchronize(c->stream));
-  return QBC_OK;
+  return two ? read_stats(c, stats) : QBC_OK;
 }
+}  // namespace
 
 extern "C" int qbc_trace_rays(qbc_ctx* c, const float* pos, const float* dir, int64_t n, const float basecube[4],
                               int maxlevel, const qbc_ray_hits* out, int on_device) {
@@ -779,14 +898,14 @@ int noalloc_queues(int device, unsigned int** out) {
 
 template <bool EXACT, bool DYN>
 int launch_render_noalloc(qbc_ctx* c, const qbc::Batch& b, size_t smem, unsigned int* queue) {
-  auto kern = qbc::render_kernel<EXACT, DYN>;
+  auto kern = qbc::render_kernel<EXACT, DYN, qbc::kFused, false>;
   QBC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
   int per_sm = 0;
   QBC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, qbc::kThreads, smem));
   if (per_sm < 1) return fail(QBC_E_STATE, "render_kernel: no block fits on an SM with %zu B shared memory", smem);
   int64_t blocks = std::min<int64_t>((int64_t)per_sm * c->sm_count, ((int64_t)b.tiles_total + 3) / 4);
   blocks = std::max<int64_t>(blocks, 1);
-  kern<<<(unsigned)blocks, qbc::kThreads, smem, c->stream>>>(device_scene(c), b, queue);
+  kern<<<(unsigned)blocks, qbc::kThreads, smem, c->stream>>>(device_scene(c), b, queue, qbc::Wave{});
   QBC_CUDA(cudaGetLastError());
   ++c->launches;
   return QBC_OK;

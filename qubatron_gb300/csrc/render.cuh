@@ -16,14 +16,14 @@ namespace qbc {
 
 constexpr int kThreads = 128;  // 4 warps
 constexpr int kMaxViewsPerLaunch = 32;
-constexpr int kPixWords = 26;  // per-lane pixel state words in shared memory
+constexpr int kPixWords = 28;  // per-lane pixel state words in shared memory
 
 struct ViewJob {
   qbc_view v;
   qbc_outputs o;  // device pointers
-  int32_t tiles_x;     // 8-pixel-wide warp tiles per row
-  int32_t tile_begin;  // first global tile index of this view
-  int32_t pad[2];
+  int32_t tiles_x;      // 8-pixel-wide warp tiles per row
+  int32_t tile_begin;   // first global tile index of this view
+  int64_t pixel_begin;  // first pixel index of this view within the batch
 };
 
 struct Batch {
@@ -69,7 +69,9 @@ __device__ __forceinline__ float4 view_bc(const qbc_view& v) {
   return make_float4(v.basecube[0], v.basecube[1], v.basecube[2], v.basecube[3]);
 }
 
-// Per-lane pixel state in shared memory, word k at px[k * kThreads].
+// Per-lane pixel state in shared memory, word k at px[k * kThreads]. The
+// first kRecCopy words are also the record a primary pass hands to the
+// shade pass.
 enum PixWord : int {
   kPxView = 0, kPxXY, kPxFlags,
   kPxCsv,                  // 3 words: camera ray direction
@@ -78,11 +80,42 @@ enum PixWord : int {
   kPxNrm = kPxCol + 4,     // 3 words: primary normal
   kPxLeaf = kPxNrm + 3,    // 4 words: primary leaf s, d; shadow leaf s, d
   kPxVis = kPxLeaf + 4,    // 4 words: visits primary s, d; shadow s, d
-  kPxEnd = kPxVis + 4
+  kPxProp = kPxVis + 4,    // 3 words: proposed shadow-ray t of the shade pass
+  kPxEnd = kPxProp + 3
 };
+constexpr int kRecCopy = kPxProp;  // words a record carries from the primary pass
 static_assert(kPxEnd <= kPixWords, "pixel state");
 
-enum Phase : int { kIdle = 0, kPrimary = 1, kShadow = 2, kFlare = 3 };
+// Records of the two-pass render: 32 words per shaded or flare pixel.
+constexpr int kRecWords = 32;
+constexpr int kRecProp = kPxProp;      // 3 floats: proposals (written between the passes)
+constexpr int kRecLogT = kPxProp + 3;  // float: t of the plain shadow walk's first leaf, -1 if none
+constexpr int kRecLogLit = kRecLogT + 1;  // lit bit of the plain shadow walk
+
+enum Phase : int { kIdle = 0, kPrimary = 1, kShadow = 2, kFlare = 3, kProposal = 4 };
+enum Mode : int { kFused = 0, kPrimaryPass = 1, kShadePass = 2 };
+
+// Statistics of the shade pass (uint64 each).
+enum Stat : int {
+  kStatShadowRays = 0,   // plain shadow walks
+  kStatShadowVisits,     // node visits of plain shadow walks
+  kStatPropTried,        // proposal walks
+  kStatPropProven,       // shadow rays settled by a proposal
+  kStatPropVisits,       // node visits of proposal walks
+  kStatCount = 8
+};
+
+struct Wave {
+  uint32_t* rec;                // records (kRecWords words each)
+  unsigned int* qcount;         // records written by the primary pass
+  unsigned int* qnext;          // shade-pass work counter
+  unsigned long long* stats;    // kStatCount counters
+  uint32_t cap;                 // record capacity
+  int32_t log;                  // shade pass: log the plain walk's first leaf
+  int32_t nprop;                // proposals per record to try (0..3)
+  int32_t pdepth;               // level of the proposed cells
+  float* pixlog;                // per pixel of the batch: logged first-leaf t (-1 none), when log
+};
 
 // Internal flag: the pixel's camera ray is within the flare angle. The public
 // QBC_PX_FLARE_TEST is set only when the flare ray is actually traced.
@@ -94,20 +127,50 @@ struct PixRef {
   __device__ __forceinline__ float& f(int k) const { return reinterpret_cast<float&>(base[k * kThreads]); }
 };
 
-template <bool EXACT, bool DYN>
+// Octets of a point down to `depth` levels (octree.c:100-109), root first.
+__device__ __forceinline__ uint32_t point_path(float3 q, float basesize, int depth) {
+  uint32_t k = 0;
+  float size = basesize;
+  for (int level = 0; level < depth; ++level) {
+    size /= 2.0f;
+    int octet = (int)(q.x / size) % 2;
+    int yi = (int)(q.y / size) % 2;
+    int zi = (int)(q.z / size) % 2;
+    if (yi == 0) octet += 2;
+    if (zi == 0) octet += 4;
+    k = (k << 3) | (uint32_t)octet;
+  }
+  return k;
+}
+
+template <bool EXACT, bool DYN, int MODE, bool PROP>
 struct Shader {
   const DevScene& sc;
   const Batch& batch;
+  const Wave& wave;
   Stack st;
   PixRef px;
-  Walker<EXACT, DYN> w;
+  Walker<EXACT, DYN, PROP> w;
   int phase;     // kind of the lane's current ray, kIdle without a pixel
   bool running;  // the ray is being walked
+  bool enqueue;  // primary pass: the pixel goes to the shade pass
   int result;    // status of the ray once it ended
   int maxlevel;
+  int prop_k;    // next proposal to try
+  uint32_t rec_q;  // shade pass: record of the pixel
+  uint32_t next_target;
+  int next_tdepth;
   float4 bc;
+  unsigned long long stat[kStatCount];
 
   __device__ __forceinline__ const qbc_view& view() const { return batch.job[px.w(kPxView)].v; }
+
+  // Index of the pixel among all pixels of the batch (views in order).
+  __device__ __forceinline__ int64_t pixel_index() const {
+    const ViewJob& J = batch.job[px.w(kPxView)];
+    const uint32_t xy = px.w(kPxXY);
+    return J.pixel_begin + (int64_t)(xy >> 16) * J.v.width_px + (xy & 0xFFFFu);
+  }
 
   __device__ __forceinline__ void write_out(float4 col) {
     const ViewJob& J = batch.job[px.w(kPxView)];
@@ -167,21 +230,98 @@ struct Shader {
     rd = csv;
   }
 
+  // Shadow ray of the pixel in smem: from the light to the primary hit.
+  __device__ __forceinline__ void shadow_ray(float3& rp, float3& rd) const {
+    const qbc_view& v = view();
+    rp = make_float3(v.light[0], v.light[1], v.light[2]);
+    rd = make_float3(px.f(kPxIsp) - rp.x, px.f(kPxIsp + 1) - rp.y, px.f(kPxIsp + 2) - rp.z);
+  }
+
+  // The next usable proposal from prop_k on: the level-pdepth cell around
+  // the proposed point of the shadow ray. Returns false when none is left.
+  __device__ __forceinline__ bool next_proposal(float3 rp, float3 rd) {
+    while (prop_k < wave.nprop) {
+      const float t = px.f(kPxProp + prop_k);
+      ++prop_k;
+      if (!(t > 0.0f && t < 1.0f)) continue;
+      const float3 q = make_float3(rp.x + rd.x * t, rp.y + rd.y * t, rp.z + rd.z * t);
+      const float s = bc.w;
+      if (!(q.x >= bc.x && q.x < bc.x + s && q.y >= bc.y - s && q.y < bc.y && q.z >= bc.z - s && q.z < bc.z)) continue;
+      if (bc.x != 0.0f || bc.y != s || bc.z != s) return false;  // paths assume basecube (0, S, S, S)
+      next_tdepth = min(wave.pdepth, maxlevel);
+      next_target = point_path(q, s, next_tdepth);
+      return true;
+    }
+    return false;
+  }
+
+  // Shade pass: pixel of record q; sets its first ray into (rp, rd).
+  __device__ __forceinline__ void begin_record(uint32_t q, float3& rp, float3& rd) {
+    const uint32_t* r = wave.rec + (size_t)q * kRecWords;
+#pragma unroll
+    for (int k = 0; k < kRecCopy; ++k) px.w(k) = r[k];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) px.w(kPxProp + k) = PROP ? r[kRecProp + k] : 0u;
+    rec_q = q;
+    const qbc_view& v = view();
+    maxlevel = v.maxlevel;
+    bc = view_bc(v);
+    prop_k = 0;
+    next_tdepth = 0;
+    if (px.w(kPxFlags) & QBC_PX_SHADED) {
+      shadow_ray(rp, rd);
+      phase = kShadow;
+      if (PROP && next_proposal(rp, rd)) phase = kProposal;
+    } else {
+      start_flare(rp, rd);
+    }
+  }
+
+  __device__ __forceinline__ void start_flare(float3& rp, float3& rd) {
+    px.w(kPxFlags) |= QBC_PX_FLARE_TEST;
+    const qbc_view& v = view();
+    rp = make_float3(v.camfp[0], v.camfp[1], v.camfp[2]);
+    rd = make_float3(v.light[0] - rp.x, v.light[1] - rp.y, v.light[2] - rp.z);
+    phase = kFlare;
+  }
+
   // Flare ray (octree_fsh.c:452-459) if the pixel wants one: returns true and
   // sets (rp, rd); otherwise writes the pixel.
   __device__ __forceinline__ bool flare_or_finish(float4 col, float3& rp, float3& rd) {
     if (px.w(kPxFlags) & kWantFlare) {
-      px.w(kPxFlags) |= QBC_PX_FLARE_TEST;
-      const qbc_view& v = view();
 #pragma unroll
       for (int k = 0; k < 4; ++k) px.f(kPxCol + k) = (&col.x)[k];
-      rp = make_float3(v.camfp[0], v.camfp[1], v.camfp[2]);
-      rd = make_float3(v.light[0] - rp.x, v.light[1] - rp.y, v.light[2] - rp.z);
-      phase = kFlare;
+      start_flare(rp, rd);
       return true;
     }
     write_out(col);
     return false;
+  }
+
+  // Shading of octree_fsh.c:436-449 with the shadow walk's lit value.
+  __device__ __forceinline__ float4 shade(float lit) {
+    const qbc_view& v = view();
+    float4 pi = make_float4(px.f(kPxIsp), px.f(kPxIsp + 1), px.f(kPxIsp + 2), px.f(kPxIsp + 3));
+    float4 pc = make_float4(px.f(kPxCol), px.f(kPxCol + 1), px.f(kPxCol + 2), px.f(kPxCol + 3));
+    float3 pn = make_float3(px.f(kPxNrm), px.f(kPxNrm + 1), px.f(kPxNrm + 2));
+    float3 csv = make_float3(px.f(kPxCsv), px.f(kPxCsv + 1), px.f(kPxCsv + 2));
+    float3 lghtv = make_float3(pi.x - v.light[0], pi.y - v.light[1], pi.z - v.light[2]);
+    float3 nl = normalize3(make_float3(-lghtv.x, -lghtv.y, -lghtv.z));
+    float3 nn = normalize3(pn);
+    float3 nc = normalize3(make_float3(-csv.x, -csv.y, -csv.z));
+    float lght_nrm_ang = glsl_max(dot3(nl, nn), 0.0f);
+    float camv_nrm_ang = glsl_max(dot3(nc, nn), 0.0f);
+    if (lit != 0.0f) px.w(kPxFlags) |= QBC_PX_LIT;
+    float k = 0.1f + 0.2f * camv_nrm_ang + lght_nrm_ang * lit * 0.7f;
+    pc.x = pc.x * k;
+    pc.y = pc.y * k;
+    pc.z = pc.z * k;
+    pc.z *= 0.7f;
+    float g = (float)v.shoot * camv_nrm_ang * 0.1f;
+    pc.x += g;
+    pc.y += g;
+    pc.z += g;
+    return pc;
   }
 
   // The lane's ray ended with `result`: record it and decide the pixel's next
@@ -194,6 +334,32 @@ struct Shader {
       w.leaf(sc, ms, md, col, nrm);
       isp = w.e;
     }
+
+    if (phase == kProposal) {
+      // a proposal walk ended: a leaf well before the hit proves the shadow
+      stat[kStatPropTried] += 1;
+      stat[kStatPropVisits] += w.vis_s + w.vis_d;
+      px.w(kPxVis + 2) += w.vis_s;
+      px.w(kPxVis + 3) += w.vis_d;
+      bool proven = false;
+      if (r == kLeaf) {
+        float dx = isp.x - px.f(kPxIsp), dy = isp.y - px.f(kPxIsp + 1), dz = isp.z - px.f(kPxIsp + 2);
+        proven = isp.w < 1.0f && dx * dx + dy * dy + dz * dz > 16.0f;
+      }
+      if (proven) {
+        stat[kStatPropProven] += 1;
+        // the plain walk reaches a leaf at least this far from the hit: unlit
+        px.w(kPxFlags) |= QBC_PX_SHADOW_LEAF;
+        px.w(kPxLeaf + 2) = (uint32_t)-2;  // the plain walk's leaf was not computed
+        px.w(kPxLeaf + 3) = (uint32_t)-2;
+        return flare_or_finish(shade(0.0f), rp, rd);
+      }
+      shadow_ray(rp, rd);
+      if (next_proposal(rp, rd)) return true;  // phase stays kProposal
+      phase = kShadow;
+      return true;
+    }
+
     if (w.oob) px.w(kPxFlags) |= QBC_PX_OOB;
 
     if (phase == kPrimary) {
@@ -208,56 +374,50 @@ struct Shader {
       px.f(kPxIsp + 1) = isp.y;
       px.f(kPxIsp + 2) = isp.z;
       px.f(kPxIsp + 3) = isp.w;
-      if (isp.w > 0.0f) {
-        // shadow ray from the light to the hit (octree_fsh.c:431-432)
-        px.w(kPxFlags) |= QBC_PX_SHADED;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) px.f(kPxCol + k) = (&col.x)[k];
+      for (int k = 0; k < 4; ++k) px.f(kPxCol + k) = (&col.x)[k];
+      if (isp.w > 0.0f) {
+        px.w(kPxFlags) |= QBC_PX_SHADED;
         px.f(kPxNrm) = nrm.x;
         px.f(kPxNrm + 1) = nrm.y;
         px.f(kPxNrm + 2) = nrm.z;
-        const qbc_view& v = view();
-        rp = make_float3(v.light[0], v.light[1], v.light[2]);
-        rd = make_float3(isp.x - rp.x, isp.y - rp.y, isp.z - rp.z);
+        if (MODE == kPrimaryPass) {
+          enqueue = true;
+          return false;
+        }
+        // shadow ray from the light to the hit (octree_fsh.c:431-432)
+        shadow_ray(rp, rd);
         phase = kShadow;
         return true;
+      }
+      if (MODE == kPrimaryPass && (px.w(kPxFlags) & kWantFlare)) {
+        enqueue = true;
+        return false;
       }
       return flare_or_finish(col, rp, rd);
     }
     if (phase == kShadow) {
       // shading (octree_fsh.c:433-449)
-      px.w(kPxVis + 2) = w.vis_s;
-      px.w(kPxVis + 3) = w.vis_d;
+      stat[kStatShadowRays] += 1;
+      stat[kStatShadowVisits] += w.vis_s + w.vis_d;
+      px.w(kPxVis + 2) += w.vis_s;
+      px.w(kPxVis + 3) += w.vis_d;
       if (r == kLeaf) {
         px.w(kPxFlags) |= QBC_PX_SHADOW_LEAF;
         px.w(kPxLeaf + 2) = (uint32_t)w.ns;
         px.w(kPxLeaf + 3) = (uint32_t)w.nd;
       }
-      const qbc_view& v = view();
-      float4 pi = make_float4(px.f(kPxIsp), px.f(kPxIsp + 1), px.f(kPxIsp + 2), px.f(kPxIsp + 3));
-      float4 pc = make_float4(px.f(kPxCol), px.f(kPxCol + 1), px.f(kPxCol + 2), px.f(kPxCol + 3));
-      float3 pn = make_float3(px.f(kPxNrm), px.f(kPxNrm + 1), px.f(kPxNrm + 2));
-      float3 csv = make_float3(px.f(kPxCsv), px.f(kPxCsv + 1), px.f(kPxCsv + 2));
-      float3 lghtv = make_float3(pi.x - v.light[0], pi.y - v.light[1], pi.z - v.light[2]);
-      float ix = isp.x - pi.x, iy = isp.y - pi.y, iz = isp.z - pi.z;
+      float ix = isp.x - px.f(kPxIsp), iy = isp.y - px.f(kPxIsp + 1), iz = isp.z - px.f(kPxIsp + 2);
       float sqr = ix * ix + iy * iy + iz * iz;
-      float3 nl = normalize3(make_float3(-lghtv.x, -lghtv.y, -lghtv.z));
-      float3 nn = normalize3(pn);
-      float3 nc = normalize3(make_float3(-csv.x, -csv.y, -csv.z));
-      float lght_nrm_ang = glsl_max(dot3(nl, nn), 0.0f);
-      float camv_nrm_ang = glsl_max(dot3(nc, nn), 0.0f);
       float lit = (15.0f < sqr) ? 0.0f : 1.0f;  // step(sqr, 15.0)
-      if (lit != 0.0f) px.w(kPxFlags) |= QBC_PX_LIT;
-      float k = 0.1f + 0.2f * camv_nrm_ang + lght_nrm_ang * lit * 0.7f;
-      pc.x = pc.x * k;
-      pc.y = pc.y * k;
-      pc.z = pc.z * k;
-      pc.z *= 0.7f;
-      float g = (float)v.shoot * camv_nrm_ang * 0.1f;
-      pc.x += g;
-      pc.y += g;
-      pc.z += g;
-      return flare_or_finish(pc, rp, rd);
+      if (MODE == kShadePass && wave.log) {
+        uint32_t* rq = wave.rec + (size_t)rec_q * kRecWords;
+        const float lt = r == kLeaf ? isp.w : -1.0f;
+        reinterpret_cast<float&>(rq[kRecLogT]) = lt;
+        rq[kRecLogLit] = lit != 0.0f ? 1u : 0u;
+        if (wave.pixlog) wave.pixlog[pixel_index()] = lit != 0.0f ? -1.0f : lt;
+      }
+      return flare_or_finish(shade(lit), rp, rd);
     }
     // flare ray ended (octree_fsh.c:456-458)
     const qbc_view& v = view();
@@ -292,21 +452,35 @@ __device__ __forceinline__ int tile_view(const Batch& b, int tile) {
 // a time.
 constexpr int kServiceMinDefault = 4;
 
-template <bool EXACT, bool DYN>
+// MODE kFused: every pixel's primary ray, shadow ray, shading and flare.
+// MODE kPrimaryPass: primary rays only; shaded and flare pixels go to the
+// record queue (warp-aggregated atomics), the rest are written.
+// MODE kShadePass: the queued pixels' shadow rays (first the proposals, with
+// PROP), shading and flare.
+template <bool EXACT, bool DYN, int MODE, bool PROP>
 __global__ void __launch_bounds__(kThreads) render_kernel(DevScene sc, const __grid_constant__ Batch batch,
-                                                          unsigned int* queue) {
+                                                          unsigned int* queue, const __grid_constant__ Wave wave) {
   extern __shared__ uint32_t smem[];
   const int tid = threadIdx.x, lane = tid & 31;
-  constexpr int kW = Walker<EXACT, DYN>::kWords;
-  Shader<EXACT, DYN> S{sc, batch, Stack{smem + tid, kThreads}, PixRef{smem + kW * batch.max_level * kThreads + tid}};
+  constexpr int kW = Walker<EXACT, DYN, PROP>::kWords;
+  Shader<EXACT, DYN, MODE, PROP> S{sc, batch, wave, Stack{smem + tid, kThreads},
+                                   PixRef{smem + kW * batch.max_level * kThreads + tid}};
   S.phase = kIdle;
   S.running = false;
+  S.enqueue = false;
   S.result = 0;
   S.maxlevel = 0;
+  S.prop_k = 0;
+  S.rec_q = 0;
+  S.next_target = 0;
+  S.next_tdepth = 0;
   S.bc = make_float4(0.f, 0.f, 0.f, 0.f);
-  int tile = 0, consumed = 32;  // warp-uniform
+#pragma unroll
+  for (int k = 0; k < kStatCount; ++k) S.stat[k] = 0;
+  int chunk = 0, consumed = 32;  // warp-uniform
   bool exhausted = false;
   const unsigned lt_mask = (1u << lane) - 1u;
+  const unsigned total = MODE == kShadePass ? min(*wave.qcount, wave.cap) : (unsigned)batch.tiles_total;
 
   for (;;) {
     const unsigned run = __ballot_sync(0xFFFFFFFFu, S.running);
@@ -316,14 +490,33 @@ __global__ void __launch_bounds__(kThreads) render_kernel(DevScene sc, const __g
       float3 rp = make_float3(0.f, 0.f, 0.f), rd = rp;
       bool go = false;
       if (!S.running && S.phase != kIdle) go = S.consume(rp, rd);
+      if (MODE == kPrimaryPass) {
+        // hand shaded / flare pixels to the shade pass: one atomic per warp
+        const unsigned enq = __ballot_sync(0xFFFFFFFFu, S.enqueue);
+        if (enq) {
+          unsigned base = 0;
+          if (lane == __ffs(enq) - 1) base = atomicAdd(wave.qcount, (unsigned)__popc(enq));
+          base = __shfl_sync(0xFFFFFFFFu, base, __ffs(enq) - 1);
+          if (S.enqueue) {
+            const unsigned q = base + __popc(enq & lt_mask);
+            if (q < wave.cap) {
+              uint32_t* r = wave.rec + (size_t)q * kRecWords;
+#pragma unroll
+              for (int k = 0; k < kRecCopy; ++k) r[k] = S.px.w(k);
+            }
+            S.enqueue = false;
+            S.phase = kIdle;
+          }
+        }
+      }
       unsigned idle = __ballot_sync(0xFFFFFFFFu, S.phase == kIdle);
       while (idle && !exhausted) {
         if (consumed >= 32) {
           unsigned t0 = 0;
-          if (lane == 0) t0 = atomicAdd(queue, 1u);
-          tile = (int)__shfl_sync(0xFFFFFFFFu, t0, 0);
+          if (lane == 0) t0 = atomicAdd(MODE == kShadePass ? wave.qnext : queue, MODE == kShadePass ? 32u : 1u);
+          chunk = (int)__shfl_sync(0xFFFFFFFFu, t0, 0);
           consumed = 0;
-          if (tile >= batch.tiles_total) {
+          if ((unsigned)chunk >= total) {
             exhausted = true;
             break;
           }
@@ -332,24 +525,37 @@ __global__ void __launch_bounds__(kThreads) render_kernel(DevScene sc, const __g
         const int rank = __popc(idle & lt_mask);
         if (((idle >> lane) & 1u) && rank < avail) {
           const int slot = consumed + rank;
-          const int vi = tile_view(batch, tile);
-          const ViewJob& J = batch.job[vi];
-          const int t = tile - J.tile_begin;
-          const int x = (t % J.tiles_x) * 8 + (slot & 7);
-          const int y = (t / J.tiles_x) * 4 + (slot >> 3);
-          if (x < J.v.width_px && y < J.v.height_px) {
-            S.begin_pixel(vi, x, y, rp, rd);
-            go = true;
+          if (MODE == kShadePass) {
+            const unsigned q = (unsigned)chunk + slot;
+            if (q < total) {
+              S.begin_record(q, rp, rd);
+              go = true;
+            }
+          } else {
+            const int vi = tile_view(batch, chunk);
+            const ViewJob& J = batch.job[vi];
+            const int t = chunk - J.tile_begin;
+            const int x = (t % J.tiles_x) * 8 + (slot & 7);
+            const int y = (t / J.tiles_x) * 4 + (slot >> 3);
+            if (x < J.v.width_px && y < J.v.height_px) {
+              S.begin_pixel(vi, x, y, rp, rd);
+              go = true;
+            }
           }
         }
         consumed += min(avail, __popc(idle));
         idle = __ballot_sync(0xFFFFFFFFu, S.phase == kIdle);
       }
       if (go) {
-        if (S.w.start(S.bc, rp, rd) == kDiscard)
+        if (S.w.start(S.bc, rp, rd) == kDiscard) {
           S.discard();
-        else
+        } else {
           S.running = true;
+          if (PROP && S.phase == kProposal) {
+            S.w.target = S.next_target;
+            S.w.tdepth = S.next_tdepth;
+          }
+        }
       }
       if (exhausted && __ballot_sync(0xFFFFFFFFu, S.phase != kIdle) == 0) break;
     }
@@ -359,6 +565,48 @@ __global__ void __launch_bounds__(kThreads) render_kernel(DevScene sc, const __g
         S.running = false;
         S.result = r;
       }
+    }
+  }
+  if (MODE == kShadePass) {
+    // statistics: one atomic per warp and counter
+#pragma unroll
+    for (int k = 0; k < kStatCount; ++k) {
+      unsigned long long v = S.stat[k];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+      if (lane == 0 && v) atomicAdd(wave.stats + k, v);
+    }
+  }
+}
+
+// Proposals for the records of a two-pass render: the t of the first leaf a
+// previous plain walk of the same pixel logged (when it shadowed), or seeded
+// pseudo-random t values (exactness tests exercise the proposal path with
+// both).
+__global__ void fill_logged_proposals(const __grid_constant__ Batch batch, const __grid_constant__ Wave wave) {
+  const unsigned total = min(*wave.qcount, wave.cap);
+  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+    uint32_t* r = wave.rec + (size_t)q * kRecWords;
+    const ViewJob& J = batch.job[r[kPxView]];
+    const uint32_t xy = r[kPxXY];
+    const float t = wave.pixlog[J.pixel_begin + (int64_t)(xy >> 16) * J.v.width_px + (xy & 0xFFFFu)];
+    reinterpret_cast<float&>(r[kRecProp]) = t;
+    reinterpret_cast<float&>(r[kRecProp + 1]) = -1.0f;
+    reinterpret_cast<float&>(r[kRecProp + 2]) = -1.0f;
+  }
+}
+
+__global__ void fill_random_proposals(const __grid_constant__ Wave wave, unsigned long long seed) {
+  const unsigned total = min(*wave.qcount, wave.cap);
+  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+    uint32_t* r = wave.rec + (size_t)q * kRecWords;
+    unsigned long long z = seed + 0x9E3779B97F4A7C15ull * (r[kPxXY] + 0x10001ull * r[kPxView] + 1);
+    for (int k = 0; k < 3; ++k) {
+      z += 0x9E3779B97F4A7C15ull;
+      unsigned long long x = z;
+      x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+      x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+      x ^= x >> 31;
+      reinterpret_cast<float&>(r[kRecProp + k]) = (float)(x >> 40) * (1.0f / 16777216.0f);
     }
   }
 }

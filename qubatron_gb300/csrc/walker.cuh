@@ -21,7 +21,7 @@ namespace qbc {
 
 enum : int { kRunning = 3 };
 
-template <bool EXACT, bool DYN>
+template <bool EXACT, bool DYN, bool PROP = false>
 struct Walker {
   float3 p, d;   // ray origin and direction
   float4 e0;     // entry point of the basecube
@@ -32,6 +32,11 @@ struct Walker {
   int pushes;
   bool oob;
   uint32_t vis_s, vis_d;
+  // proposal test (PROP only): while level < tdepth the walk goes straight
+  // to the cell of path `target` (3 bits per level, root first) through the
+  // candidate the plain walk would use; below it, pops stop at tdepth.
+  uint32_t target;
+  int tdepth;
 
   static constexpr int kWords = DYN ? 3 : 2;
 
@@ -51,6 +56,8 @@ struct Walker {
     oob = false;
     vis_s = 0;
     vis_d = 0;
+    target = 0;
+    tdepth = 0;
     float4 cb = brb_of(bc);
     int hitc = 0;
     float4 h0 = make_float4(0.f, 0.f, 0.f, 0.f), h1 = h0, a;
@@ -208,12 +215,22 @@ struct Walker {
     pk |= (uint32_t)len << 20;
 
     int nx = 0;
+    if (PROP && level < tdepth) {
+      // directed descent: the first candidate into the target's octet; if
+      // there is none, the plain walk never enters the target cell here
+      const int want = (int)(target >> (3 * (tdepth - 1 - level))) & 7;
+      nx = -1;
+#pragma unroll
+      for (int k = 3; k >= 0; --k)
+        if (k < len && (list_entry(pk, k) & 7) == want) nx = k;
+      if (nx < 0) return kMiss;
+    }
     float4 isp;
     int32_t cs, cd = 0;
     int cc;
     if (len > 0) {
       // ---- descend into the nearest candidate (:334-367) ----
-      cc = pk & 31;
+      cc = PROP ? list_entry(pk, nx) : (int)(pk & 31);
       int src = cc >> 3;
       isp = src == 0 ? e : (src == 1 ? hz : (src == 2 ? hx : hy));
       cs = pick8(s0, s1, cc & 7);
@@ -223,7 +240,7 @@ struct Walker {
     } else {
       // ---- pop until a level has candidates left (:368-375) ----
       for (;;) {
-        if (level == 0) return kMiss;
+        if (level == (PROP ? tdepth : 0)) return kMiss;
         --level;
         pk = slot(st, level, 0);
         nx = list_next(pk);

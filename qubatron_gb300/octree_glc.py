@@ -133,6 +133,24 @@ class OctreeGLC:
         oarr = (Outputs * n)(*outputs)
         check(self._lib.qbc_render_views(self.handle, varr, oarr, n, 1 if on_device else 0))
 
+    def render_views_ex(self, views: Sequence[View], outputs: Sequence[Outputs], on_device: bool,
+                        two_pass: bool = False, proposals: int = 0, log: bool = False, proposal_level: int = 0,
+                        seed: int = 0) -> dict:
+        """qbc_render_views_ex; returns the render statistics."""
+        n = len(views)
+        varr = (View * n)(*views)
+        oarr = (Outputs * n)(*outputs)
+        opts = _lib.RenderOpts(int(two_pass), int(proposals), int(log), int(proposal_level), int(seed))
+        st = _lib.RenderStats()
+        check(self._lib.qbc_render_views_ex(self.handle, varr, oarr, n, 1 if on_device else 0, C.byref(opts),
+                                            C.byref(st)))
+        return st.as_dict()
+
+    def render_host_ex(self, views: Sequence[View], streams: Iterable[str] = ("rgba8",), **kw):
+        bufs = [FrameBuffers(v, streams) for v in views]
+        stats = self.render_views_ex(views, [b.outputs() for b in bufs], False, **kw)
+        return bufs, stats
+
     def render_views_noalloc(self, views: Sequence[View], outputs: Sequence[Outputs]) -> None:
         """qbc_render_views_noalloc: device outputs only, no allocation in
         the call (the work-queue counters live in static device memory)."""
