@@ -241,9 +241,10 @@ def run_reference(args):
     return 0
 
 
-def measure_e2e(ctx, views, rays, world, flush, steps, update=None):
+def measure_e2e(ctx, views, rays, world, flush, steps, update=None, render=None):
     """Same views through the public C ABI into pinned host buffers: the
     timed call includes the kernel and the copy of every frame to the host."""
+    render = render or (lambda v, o, dev: ctx.render_views(v, o, on_device=dev))
     import torch
     import qubatron_gb300 as qb
     host = [torch.empty((v.height_px, v.width_px, 4), dtype=torch.uint8, pin_memory=True) for v in views]
@@ -253,7 +254,7 @@ def measure_e2e(ctx, views, rays, world, flush, steps, update=None):
         o.rgba8 = h.data_ptr()
         houts.append(o)
     for _ in range(2):
-        ctx.render_views(views, houts, on_device=False)
+        render(views, houts, False)
     e2e_t = []
     for k in range(max(3, steps)):
         flush.zero_()
@@ -261,7 +262,7 @@ def measure_e2e(ctx, views, rays, world, flush, steps, update=None):
         t0 = time.perf_counter()
         if update:
             update(k)
-        ctx.render_views(views, houts, on_device=False)
+        render(views, houts, False)
         e2e_t.append(time.perf_counter() - t0)
     e2e_s = statistics.mean(e2e_t)
     d2h = sum(h.numel() for h in host)
@@ -292,6 +293,39 @@ def run_gpu(args):
     ctx.upload_octree(False, scene.nodes)
     if args.service_min:
         ctx.set_option(qb._lib.OPT_SERVICE_MIN, args.service_min)
+
+    def render_plain(v, o, dev):
+        ctx.render_views(v, o, on_device=dev)
+
+    def render_two_pass(v, o, dev):
+        ctx.render_views_ex(v, o, dev, two_pass=True)
+
+    def render_mlp(v, o, dev):
+        ctx.render_views_ex(v, o, dev, two_pass=True, proposals=qb._lib.PROPOSE_MLP, proposal_level=args.proposal_level)
+
+    render = render_plain
+    training = None
+    if w.train_poses:
+        # occluder-proposal network: log the plain shadow walks of the
+        # training poses, train on them (both untimed), render the held-out
+        # poses with its proposals
+        from qubatron_gb300 import scenes as _sc
+        tv = _sc.train_views(w)
+        t0 = time.time()
+        samples = 0
+        for i in range(0, len(tv), 32):
+            samples = ctx.proposal_collect(tv[i:i + 32])
+        collect_s = time.time() - t0
+        t0 = time.time()
+        st = ctx.proposal_train(steps=args.train_steps, batch=8192, lr=2e-3, seed=1)
+        torch.cuda.synchronize()
+        training = {"poses": len(tv), "pose_size": "%dx%d" % w.train_size, "samples": samples,
+                    "occluded": st["occluded"], "steps": args.train_steps, "batch": 8192,
+                    "loss_first": st["loss_first"], "loss_last": st["loss_last"],
+                    "collect_s": round(collect_s, 2), "train_s": round(time.time() - t0, 2),
+                    "gate_per_mille": args.proposal_gate, "proposal_level": args.proposal_level}
+        ctx.set_option(qb._lib.OPT_PROPOSAL_GATE, args.proposal_gate)
+        render = render_mlp
 
     # device outputs
     frames = [torch.empty((v.height_px, v.width_px, 4), dtype=torch.uint8, device="cuda") for v in views]
@@ -342,34 +376,59 @@ def run_gpu(args):
     del flags, visits
 
     flush = torch.empty(2 * L2_BYTES, dtype=torch.uint8, device="cuda")
-    for f in range(args.warmup):
-        update(f)
-        ctx.render_views(views, outs, on_device=True)
-    torch.cuda.synchronize()
 
-    l0 = ctx.launch_count()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        for k in range(args.steps):
-            flush.zero_()
-            ev[k][0].record(stream)
-            update(args.warmup + k)
-            ctx.render_views(views, outs, on_device=True)
-            ev[k][1].record(stream)
+    def timed(render_fn):
+        for f in range(args.warmup):
+            update(f)
+            render_fn(views, outs, True)
         torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    launches = ctx.launch_count() - l0
-    step_ms = [a.elapsed_time(b) for a, b in ev]
+        l0 = ctx.launch_count()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        with ClockSampler(local) as clk:
+            for k in range(args.steps):
+                flush.zero_()
+                ev[k][0].record(stream)
+                update(args.warmup + k)
+                render_fn(views, outs, True)
+                ev[k][1].record(stream)
+            torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        return [a.elapsed_time(b) for a, b in ev], ctx.launch_count() - l0, clk
+
+    step_ms, launches, clk = timed(render)
     ms = statistics.mean(step_ms)
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     value = world * sum(frame_rays) / (sum(step_ms) / 1000.0) / 1e6
+
+    proposal = None
+    if training is not None:
+        # the same frames without the network (fused kernel, and the same
+        # two-pass pipeline), and the proposal statistics of one frame
+        plain_ms, _, _ = timed(render_plain)
+        two_ms, _, _ = timed(render_two_pass)
+        st_mlp = ctx.render_views_ex(views, outs, True, two_pass=True, proposals=qb._lib.PROPOSE_MLP,
+                                     proposal_level=args.proposal_level)
+        st_two = ctx.render_views_ex(views, outs, True, two_pass=True)
+        vis_mlp = st_mlp["shadow_visits"] + st_mlp["proposal_visits"]
+        mrays = lambda xs: sum(frame_rays) / (sum(xs) / 1000.0) / 1e6
+        proposal = {
+            "training": training,
+            "plain_fused_mrays": mrays(plain_ms), "plain_two_pass_mrays": mrays(two_ms), "mlp_mrays": value,
+            "speedup_vs_plain_fused": statistics.mean(plain_ms) / statistics.mean(step_ms),
+            "speedup_vs_plain_two_pass": statistics.mean(two_ms) / statistics.mean(step_ms),
+            "shadow_rays": st_two["shadow_rays"], "proposals_tried": st_mlp["proposals_tried"],
+            "proposals_proven": st_mlp["proposals_proven"],
+            "hit_rate": st_mlp["proposals_proven"] / max(1, st_mlp["proposals_tried"]),
+            "shadow_visits_plain": st_two["shadow_visits"], "shadow_visits_mlp": vis_mlp,
+            "visits_saved_frac": 1.0 - vis_mlp / max(1, st_two["shadow_visits"]),
+        }
 
     update_ms = None
     if chars:
@@ -385,7 +444,7 @@ def run_gpu(args):
     e2e = None
     if not args.no_e2e:
         e2e = measure_e2e(ctx, views, rays, world, flush, args.steps,
-                          (lambda k: update(args.warmup + k % args.steps)) if chars else None)
+                          (lambda k: update(args.warmup + k % args.steps)) if chars else None, render)
 
     hbm, peak_kind = peaks()
 
@@ -420,6 +479,9 @@ def run_gpu(args):
         "clocks": clk.summary(),
         "step_ms": [round(x, 4) for x in step_ms],
     }
+    if proposal is not None:
+        line["config"]["per_step"] = "two-pass render with occluder-network proposals (network evaluated every step)"
+        line["proposal"] = proposal
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_sample(scene, views, budget_s=args.cpu_seconds,
                                                             character=character, frame=args.warmup).items()
@@ -443,6 +505,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--service-min", type=int, default=0, help="override the kernel's service threshold")
     ap.add_argument("--workload", default=None)
+    ap.add_argument("--train-steps", type=int, default=4000, help="occluder-network training steps")
+    ap.add_argument("--proposal-gate", type=int, default=500, help="occlusion probability (per mille) to try")
+    ap.add_argument("--proposal-level", type=int, default=8, help="octree level of the proposed cells")
     args = ap.parse_args()
     global WORKLOAD
     if args.workload:

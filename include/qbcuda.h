@@ -290,6 +290,55 @@ typedef struct qbc_render_stats
 
 int qbc_render_views_ex(qbc_ctx* ctx, const qbc_view* views, const qbc_outputs* outs, int n, int outputs_on_device, const qbc_render_opts* opts, qbc_render_stats* stats);
 
+/*
+ * Occluder-proposal network (QBC_PROPOSE_MLP; not part of the reference).
+ * A 45 -> 128 -> 128 -> 128 -> 4 GELU network, BF16 weights and activations
+ * on the tensor cores with FP32 accumulation, trained on the GPU. Input of a
+ * shaded pixel: its hit point normalised to the basecube, unit normal, unit
+ * direction to the light and sin/cos of pi times the normalised hit point
+ * scaled by 4, 8, ..., 128 (6 frequencies). Output: 3 points t along the
+ * shadow ray (light at 0, hit at 1; outside (0, 1) means "no proposal") and
+ * the logit of "occluded before the hit" that gates them.
+ *
+ * qbc_proposal_collect: render views (at most 32) with the plain shadow walk
+ *   and append one sample per shaded pixel to the context's training set:
+ *   the features and the t of the walk's first leaf (occluded) or "lit".
+ * qbc_proposal_train: minibatch Adam over the training set (initialises the
+ *   network from opts->seed on first use).
+ * Parameters are QBC_PROPOSAL_PARAMS floats: W1 [128][48], b1, W2 [128][128],
+ * b2, W3 [128][128], b3, W4 [16][128], b4 [16] (W as [out][in]; input
+ * columns 45..47 and output rows 3..15 are padding).
+ */
+#define QBC_PROPOSAL_PARAMS 41360
+typedef struct qbc_train_opts
+{
+    int32_t  steps;
+    int32_t  batch;
+    float    lr;
+    int32_t  pad;
+    uint64_t seed;
+} qbc_train_opts;
+
+typedef struct qbc_train_stats
+{
+    uint64_t samples;   /* training-set size */
+    uint64_t occluded;  /* samples with an occluder */
+    float    loss_first;
+    float    loss_last; /* mean of the last 10 steps */
+} qbc_train_stats;
+
+int qbc_proposal_collect(qbc_ctx* ctx, const qbc_view* views, int n, int64_t* samples);
+int qbc_proposal_train(qbc_ctx* ctx, const qbc_train_opts* opts, qbc_train_stats* stats);
+int qbc_proposal_clear(qbc_ctx* ctx);
+int qbc_proposal_get_params(qbc_ctx* ctx, float* params);
+int qbc_proposal_set_params(qbc_ctx* ctx, const float* params);
+/* Network outputs for m host feature rows (45 floats each) -> out (4 per
+ * row: the 3 proposed t, the occlusion logit). */
+int qbc_proposal_eval(qbc_ctx* ctx, const float* x, int64_t m, float* out);
+/* Mean training loss and its gradient (QBC_PROPOSAL_PARAMS floats) for m host
+ * rows: features x (45 each), target t and kind (1 occluded at t, 0 lit). */
+int qbc_proposal_gradient(qbc_ctx* ctx, const float* x, const float* t, const int8_t* kind, int64_t m, float* loss, float* grad);
+
 /* Run the context's work on this CUDA stream (a cudaStream_t; NULL = the
  * context's own stream). */
 int qbc_set_stream(qbc_ctx* ctx, void* stream);
@@ -300,8 +349,12 @@ int qbc_synchronize(qbc_ctx* ctx);
  *   QBC_OPT_SERVICE_MIN  1..32, default 4: in the persistent render kernel a
  *   lane whose ray ended waits until this many lanes of its warp wait (or no
  *   ray runs) before the warp starts their next rays together.
+ *   QBC_OPT_PROPOSAL_GATE  0..999 per mille, default 500: QBC_PROPOSE_MLP
+ *   tries a pixel's proposals only when the network's occlusion probability
+ *   is at least this (0: always).
  */
 #define QBC_OPT_SERVICE_MIN 1
+#define QBC_OPT_PROPOSAL_GATE 2
 int qbc_set_option(qbc_ctx* ctx, int option, int value);
 int qbc_get_option(qbc_ctx* ctx, int option, int* value);
 

@@ -129,6 +129,24 @@ class RenderStats(C.Structure):
 
 
 PROPOSE_NONE, PROPOSE_MLP, PROPOSE_LOGGED, PROPOSE_RANDOM = 0, 1, 2, 3
+PROPOSAL_PARAMS = 41360
+
+
+class TrainOpts(C.Structure):
+    """qbc_train_opts."""
+
+    _fields_ = [("steps", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float), ("pad", C.c_int32),
+                ("seed", C.c_uint64)]
+
+
+class TrainStats(C.Structure):
+    """qbc_train_stats."""
+
+    _fields_ = [("samples", C.c_uint64), ("occluded", C.c_uint64), ("loss_first", C.c_float),
+                ("loss_last", C.c_float)]
+
+    def as_dict(self) -> dict:
+        return {f: (float(getattr(self, f)) if "loss" in f else int(getattr(self, f))) for f, _ in self._fields_}
 
 
 class SceneDesc(C.Structure):
@@ -171,6 +189,14 @@ SIGNATURES = {
     "qbc_render_views_ex": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int, C.c_int,
                                       C.POINTER(RenderOpts), C.POINTER(RenderStats)]),
     "qbc_render_views_noalloc": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int]),
+    "qbc_proposal_collect": (C.c_int, [C.c_void_p, C.POINTER(View), C.c_int, c_int64_p]),
+    "qbc_proposal_train": (C.c_int, [C.c_void_p, C.POINTER(TrainOpts), C.POINTER(TrainStats)]),
+    "qbc_proposal_clear": (C.c_int, [C.c_void_p]),
+    "qbc_proposal_get_params": (C.c_int, [C.c_void_p, c_float_p]),
+    "qbc_proposal_set_params": (C.c_int, [C.c_void_p, c_float_p]),
+    "qbc_proposal_eval": (C.c_int, [C.c_void_p, c_float_p, C.c_int64, c_float_p]),
+    "qbc_proposal_gradient": (C.c_int, [C.c_void_p, c_float_p, c_float_p, C.POINTER(C.c_int8), C.c_int64,
+                                        c_float_p, c_float_p]),
     "qbc_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "qbc_synchronize": (C.c_int, [C.c_void_p]),
     "qbc_set_option": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
@@ -195,6 +221,7 @@ _LIB = None
 
 
 OPT_SERVICE_MIN = 1
+OPT_PROPOSAL_GATE = 2
 
 
 def lib_path() -> str:

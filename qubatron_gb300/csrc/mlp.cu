@@ -1,0 +1,498 @@
+// Occluder-proposal network: 48 -> 128 -> 128 -> 128 -> 16 (3 used), GELU,
+// BF16 weights and activations on the tensor cores with FP32 accumulation,
+// trained on the GPU with hand-written forward, backward and Adam kernels.
+//
+// Every matrix product goes through one kernel, gemm_kernel: a 64x64 output
+// tile per block of 4 warps, operands staged in shared memory in 32-deep K
+// slices, fragments loaded with ldmatrix and multiplied with
+// mma.sync.m16n8k16 (bf16 x bf16 -> f32). The epilogue adds the bias, applies
+// GELU, stores the pre-activation (for backward) and the bf16 activation, or
+// accumulates into an fp32 result with atomics (weight gradients, where the
+// reduction runs over the batch and is split across blocks).
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "mlp.h"
+#include "qbc_internal.h"
+
+using qbc::fail;
+
+namespace qbc {
+namespace mlp {
+
+// kernels launched by this thread (the context adds the difference to its
+// launch count)
+thread_local int64_t g_launches = 0;
+int64_t launches() { return g_launches; }
+
+namespace {
+
+using bf16 = __nv_bfloat16;
+
+constexpr int kTile = 64;
+constexpr int kKs = 32;          // K slice per shared-memory stage
+constexpr int kLd = kKs + 8;     // padded row: 80 B, conflict-free ldmatrix
+
+struct Epi {
+  float* C;         // fp32 output (or atomic accumulator)
+  int ldc;
+  bf16* Cb;         // bf16 output (activation)
+  int ldcb;
+  float* Z;         // fp32 pre-activation copy
+  int ldz;
+  const float* bias;
+  int gelu;
+  int atomic;
+};
+
+__device__ __forceinline__ float gelu_f(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+  const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
+  const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
+  return cdf + x * pdf;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void ldsm_x4(uint32_t addr, uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+               : "r"(addr));
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// C[M x N] = op(A)[M x K] * op(B)[K x N]. A is M x K row-major (TA false) or
+// K x M row-major (TA true); B is K x N row-major (TB false) or N x K
+// row-major (TB true). Block z handles K rows [z * kchunk, (z + 1) * kchunk).
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(128) gemm_kernel(const bf16* __restrict__ A, int lda, const bf16* __restrict__ B,
+                                                   int ldb, int M, int N, int K, int kchunk, Epi epi) {
+  __shared__ __align__(16) bf16 As[kTile][kLd];
+  __shared__ __align__(16) bf16 Bs[kTile][kLd];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int m0 = blockIdx.y * kTile, n0 = blockIdx.x * kTile;
+  const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+  float acc[2][4][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.0f;
+  const bf16 zero = __float2bfloat16(0.0f);
+
+  for (int k0 = kb; k0 < ke; k0 += kKs) {
+    // stage op(A)[m0.., k0..] as As[m][k] and op(B)[k0.., n0..] as Bs[n][k]
+    for (int e = tid; e < kTile * kKs; e += 128) {
+      const int r = e / kKs, c = e % kKs;  // r: m or n, c: k
+      const int m = m0 + r, n = n0 + r, k = k0 + c;
+      bf16 a = zero, b = zero;
+      if (m < M && k < ke) a = TA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k];
+      if (n < N && k < ke) b = TB ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n];
+      As[r][c] = a;
+      Bs[r][c] = b;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < kKs; kk += 16) {
+      uint32_t af[2][4];
+#pragma unroll
+      for (int mi = 0; mi < 2; ++mi) {
+        const int row = wm + mi * 16 + (lane & 15);
+        const int col = kk + (lane >> 4) * 8;
+        ldsm_x4(smem_u32(&As[row][col]), af[mi][0], af[mi][1], af[mi][2], af[mi][3]);
+      }
+#pragma unroll
+      for (int nj = 0; nj < 4; nj += 2) {
+        const int row = wn + nj * 8 + (lane & 7) + ((lane >> 4) << 3);
+        const int col = kk + ((lane >> 3) & 1) * 8;
+        uint32_t b0, b1, b2, b3;
+        ldsm_x4(smem_u32(&Bs[row][col]), b0, b1, b2, b3);
+#pragma unroll
+        for (int mi = 0; mi < 2; ++mi) {
+          mma_bf16(acc[mi][nj], af[mi], b0, b1);
+          mma_bf16(acc[mi][nj + 1], af[mi], b2, b3);
+        }
+      }
+    }
+    __syncthreads();
+  }
+
+  const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int mi = 0; mi < 2; ++mi) {
+#pragma unroll
+    for (int nj = 0; nj < 4; ++nj) {
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const int m = m0 + wm + mi * 16 + g + (r >> 1) * 8;
+        const int n = n0 + wn + nj * 8 + 2 * t + (r & 1);
+        if (m >= M || n >= N) continue;
+        float v = acc[mi][nj][r];
+        if (epi.atomic) {
+          atomicAdd(&epi.C[(size_t)m * epi.ldc + n], v);
+          continue;
+        }
+        if (epi.bias) v += epi.bias[n];
+        if (epi.Z) epi.Z[(size_t)m * epi.ldz + n] = v;
+        if (epi.gelu) v = gelu_f(v);
+        if (epi.C) epi.C[(size_t)m * epi.ldc + n] = v;
+        if (epi.Cb) epi.Cb[(size_t)m * epi.ldcb + n] = __float2bfloat16(v);
+      }
+    }
+  }
+}
+
+template <bool TA, bool TB>
+int gemm(const bf16* A, int lda, const bf16* B, int ldb, int64_t M, int N, int64_t K, const Epi& epi,
+         cudaStream_t s, int64_t kchunk = 0) {
+  if (M <= 0 || N <= 0 || K <= 0) return QBC_OK;
+  if (kchunk <= 0) kchunk = K;
+  kchunk = (kchunk + kKs - 1) / kKs * kKs;
+  dim3 grid((unsigned)((N + kTile - 1) / kTile), (unsigned)((M + kTile - 1) / kTile),
+            (unsigned)((K + kchunk - 1) / kchunk));
+  if (grid.y > 65535u) return fail(QBC_E_ARG, "mlp gemm: %lld rows exceed one launch", (long long)M);
+  gemm_kernel<TA, TB><<<grid, 128, 0, s>>>(A, lda, B, ldb, (int)M, N, (int)K, (int)kchunk, epi);
+  ++g_launches;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(QBC_E_CUDA, "mlp gemm launch: %s", cudaGetErrorString(e));
+  return QBC_OK;
+}
+
+// ---- elementwise kernels ----
+
+__global__ void to_bf16_kernel(const float* __restrict__ src, bf16* __restrict__ dst, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = __float2bfloat16(src[i]);
+}
+
+// Loss of the proposals o (first 3 of 16 columns) and its gradient (bf16,
+// 16 columns). kind 1: the plain shadow walk found an occluder at t: the
+// nearest output is pulled to t (winner takes all) and the others weakly.
+// kind 0: the pixel was lit: every output is pushed past 1.1 (no proposal).
+__global__ void loss_kernel(const float* __restrict__ o, const float* __restrict__ tlab,
+                            const int8_t* __restrict__ kind, int64_t M, float scale, bf16* __restrict__ dO,
+                            float* __restrict__ loss) {
+  float local = 0.0f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < M; i += (int64_t)gridDim.x * blockDim.x) {
+    float g[kOutUsed] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const float* oi = o + i * kOutPad;
+    if (kind[i] == 1) {
+      const float t = tlab[i];
+      int best = 0;
+      float bd = fabsf(oi[0] - t);
+      for (int k = 1; k < 3; ++k)
+        if (fabsf(oi[k] - t) < bd) {
+          bd = fabsf(oi[k] - t);
+          best = k;
+        }
+      for (int k = 0; k < 3; ++k) {
+        const float d = oi[k] - t;
+        const float w = k == best ? 1.0f : 0.02f;
+        local += w * d * d;
+        g[k] = 2.0f * w * d;
+      }
+    } else if (kind[i] == 0) {
+      for (int k = 0; k < 3; ++k) {
+        const float d = 1.1f - oi[k];
+        if (d > 0.0f) {
+          local += 0.5f * d * d;
+          g[k] = -d;
+        }
+      }
+    }
+    if (kind[i] == 0 || kind[i] == 1) {
+      // occluded-or-not logit: weighted binary cross-entropy
+      const float z = oi[kGate], y = kind[i] == 1 ? 1.0f : 0.0f;
+      local += kGateWeight * (fmaxf(z, 0.0f) - y * z + log1pf(expf(-fabsf(z))));
+      g[kGate] = kGateWeight * (1.0f / (1.0f + expf(-z)) - y);
+    }
+    for (int k = 0; k < kOutPad; ++k) dO[i * kOutPad + k] = __float2bfloat16(k < kOutUsed ? g[k] * scale : 0.0f);
+  }
+  for (int off = 16; off > 0; off >>= 1) local += __shfl_down_sync(0xFFFFFFFFu, local, off);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, local * scale);
+}
+
+// dZ = dA * GELU'(Z), in bf16 for the next product.
+__global__ void gelu_back_kernel(const float* __restrict__ dA, const float* __restrict__ Z, int64_t n,
+                                 bf16* __restrict__ dZ) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    dZ[i] = __float2bfloat16(dA[i] * gelu_grad(Z[i]));
+}
+
+// db[n] += sum over rows of dZ[:, n]
+__global__ void bias_grad_kernel(const bf16* __restrict__ dZ, int64_t M, int N, float* __restrict__ db) {
+  const int n = blockIdx.x;
+  float s = 0.0f;
+  for (int64_t i = threadIdx.x; i < M; i += blockDim.x) s += __bfloat162float(dZ[i * N + n]);
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xFFFFFFFFu, s, off);
+  __shared__ float part[32];
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.0f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
+    db[n] += t;
+  }
+}
+
+__global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                            float* __restrict__ v, int64_t n, float lr, float b1, float b2, float eps, float c1,
+                            float c2) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    m[i] = b1 * m[i] + (1.0f - b1) * gi;
+    v[i] = b2 * v[i] + (1.0f - b2) * gi * gi;
+    p[i] -= lr * (m[i] / c1) / (sqrtf(v[i] / c2) + eps);
+  }
+}
+
+int grid1(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 4096)); }
+
+}  // namespace
+
+// Parameter offsets (floats) in the master array: W1 b1 W2 b2 W3 b3 W4 b4,
+// each W as [out][in].
+int64_t param_offset(int layer, bool bias) {
+  const int64_t w1 = (int64_t)kHidden * kIn, w2 = (int64_t)kHidden * kHidden, w4 = (int64_t)kOutPad * kHidden;
+  const int64_t sizes[8] = {w1, kHidden, w2, kHidden, w2, kHidden, w4, kOutPad};
+  int64_t off = 0;
+  for (int k = 0; k < 2 * layer + (bias ? 1 : 0); ++k) off += sizes[k];
+  return off;
+}
+
+int64_t param_count() { return param_offset(4, false); }
+
+void Net::release() {
+  cudaFree(master);
+  cudaFree(wb);
+  cudaFree(grad);
+  cudaFree(m);
+  cudaFree(v);
+  cudaFree(work);
+  master = grad = m = v = nullptr;
+  wb = nullptr;
+  work = nullptr;
+  work_rows = 0;
+  ready = false;
+}
+
+int Net::init(uint64_t seed, cudaStream_t s) {
+  const int64_t n = param_count();
+  if (!master) {
+    cudaError_t e = cudaMalloc(&master, n * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&wb, n * 2);
+    if (e == cudaSuccess) e = cudaMalloc(&grad, n * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&m, n * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&v, n * 4);
+    if (e != cudaSuccess) return fail(QBC_E_NOMEM, "mlp parameters: %s", cudaGetErrorString(e));
+  }
+  // uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) weights from a seeded splitmix64,
+  // zero biases; padding rows / columns zero
+  std::vector<float> h(n, 0.0f);
+  uint64_t st = seed * 0x9E3779B97F4A7C15ull + 77;
+  auto u01 = [&]() {
+    uint64_t z = (st += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+  };
+  const int ins[4] = {kIn, kHidden, kHidden, kHidden}, outs[4] = {kHidden, kHidden, kHidden, kOutPad};
+  const int used_in[4] = {kInUsed, kHidden, kHidden, kHidden}, used_out[4] = {kHidden, kHidden, kHidden, kOutUsed};
+  for (int l = 0; l < 4; ++l) {
+    const double a = 1.0 / std::sqrt((double)used_in[l]);
+    float* W = h.data() + param_offset(l, false);
+    for (int o = 0; o < outs[l]; ++o)
+      for (int i = 0; i < ins[l]; ++i)
+        W[o * ins[l] + i] = (o < used_out[l] && i < used_in[l]) ? (float)((2.0 * u01() - 1.0) * a) : 0.0f;
+  }
+  // output bias: start with "no proposal" (t past the hit)
+  float* b4 = h.data() + param_offset(3, true);
+  for (int o = 0; o < kOut; ++o) b4[o] = 1.5f;
+  cudaError_t e = cudaMemcpyAsync(master, h.data(), n * 4, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(m, 0, n * 4, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(v, 0, n * 4, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return fail(QBC_E_CUDA, "mlp init: %s", cudaGetErrorString(e));
+  step_count = 0;
+  ready = true;
+  return sync_weights(s);
+}
+
+int Net::set(const float* host, cudaStream_t s) {
+  if (!master) {
+    int rc = init(1, s);
+    if (rc) return rc;
+  }
+  cudaError_t e = cudaMemcpyAsync(master, host, param_count() * 4, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return fail(QBC_E_CUDA, "mlp set: %s", cudaGetErrorString(e));
+  ready = true;
+  return sync_weights(s);
+}
+
+int Net::get(float* host, cudaStream_t s) const {
+  if (!master) return fail(QBC_E_STATE, "mlp: no parameters");
+  cudaError_t e = cudaMemcpyAsync(host, master, param_count() * 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return fail(QBC_E_CUDA, "mlp get: %s", cudaGetErrorString(e));
+  return QBC_OK;
+}
+
+int Net::sync_weights(cudaStream_t s) {
+  const int64_t n = param_count();
+  to_bf16_kernel<<<grid1(n), 256, 0, s>>>(master, wb, n);
+  ++g_launches;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(QBC_E_CUDA, "mlp weights: %s", cudaGetErrorString(e));
+  return QBC_OK;
+}
+
+int Net::ensure_work(int64_t rows) {
+  if (work_rows >= rows) return QBC_OK;
+  cudaFree(work);
+  work = nullptr;
+  work_rows = 0;
+  // per row: Z1..Z3 fp32, A1..A3 bf16, dA fp32, dZ bf16 (hidden wide), O fp32, dO bf16
+  const size_t per = (size_t)3 * kHidden * 4 + 3 * kHidden * 2 + kHidden * 4 + kHidden * 2 + kOutPad * 4 + kOutPad * 2;
+  cudaError_t e = cudaMalloc(&work, per * (size_t)rows + 1024);
+  if (e != cudaSuccess) return fail(QBC_E_NOMEM, "mlp work buffers for %lld rows: %s", (long long)rows,
+                                    cudaGetErrorString(e));
+  work_rows = rows;
+  return QBC_OK;
+}
+
+// Views into the work buffer for `rows` rows.
+struct Bufs {
+  float* Z[3];
+  bf16* A[3];
+  float* dA;
+  bf16* dZ;
+  float* O;
+  bf16* dO;
+};
+
+static Bufs carve(char* base, int64_t rows) {
+  Bufs b;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    char* p = base + off;
+    off += (bytes + 255) & ~size_t(255);
+    return p;
+  };
+  for (int l = 0; l < 3; ++l) b.Z[l] = (float*)take((size_t)rows * kHidden * 4);
+  for (int l = 0; l < 3; ++l) b.A[l] = (bf16*)take((size_t)rows * kHidden * 2);
+  b.dA = (float*)take((size_t)rows * kHidden * 4);
+  b.dZ = (bf16*)take((size_t)rows * kHidden * 2);
+  b.O = (float*)take((size_t)rows * kOutPad * 4);
+  b.dO = (bf16*)take((size_t)rows * kOutPad * 2);
+  return b;
+}
+
+int Net::forward(const bf16* X, int64_t rows, float* out, cudaStream_t s, bool keep) {
+  if (!ready) return fail(QBC_E_STATE, "mlp: not initialised");
+  const bf16* W[4];
+  const float* bsv[4];
+  for (int l = 0; l < 4; ++l) {
+    W[l] = wb + param_offset(l, false);
+    bsv[l] = master + param_offset(l, true);
+  }
+  const int64_t chunk = keep ? rows : std::min<int64_t>(rows, kChunkRows);
+  int rc = ensure_work(chunk);
+  if (rc) return rc;
+  for (int64_t r0 = 0; r0 < rows; r0 += chunk) {
+    const int64_t n = std::min(chunk, rows - r0);
+    Bufs b = carve((char*)work, chunk);
+    const bf16* in = X + r0 * kIn;
+    int ld = kIn;
+    for (int l = 0; l < 3; ++l) {
+      Epi e{nullptr, 0, b.A[l], kHidden, keep ? b.Z[l] : nullptr, kHidden, bsv[l], 1, 0};
+      rc = gemm<false, true>(in, ld, W[l], l == 0 ? kIn : kHidden, n, kHidden, l == 0 ? kIn : kHidden, e, s);
+      if (rc) return rc;
+      in = b.A[l];
+      ld = kHidden;
+    }
+    Epi e{out + r0 * kOutPad, kOutPad, nullptr, 0, nullptr, 0, bsv[3], 0, 0};
+    rc = gemm<false, true>(in, kHidden, W[3], kHidden, n, kOutPad, kHidden, e, s);
+    if (rc) return rc;
+  }
+  return QBC_OK;
+}
+
+int Net::gradient(const bf16* X, const float* tlab, const int8_t* kind, int64_t rows, float* loss, cudaStream_t s) {
+  int rc = ensure_work(rows);
+  if (rc) return rc;
+  Bufs b = carve((char*)work, rows);
+  rc = forward(X, rows, b.O, s, true);
+  if (rc) return rc;
+  const int64_t n = param_count();
+  if (cudaMemsetAsync(grad, 0, n * 4, s) != cudaSuccess || cudaMemsetAsync(loss, 0, 4, s) != cudaSuccess)
+    return fail(QBC_E_CUDA, "mlp gradient: memset");
+  const float scale = 1.0f / (float)rows;
+  loss_kernel<<<grid1(rows), 256, 0, s>>>(b.O, tlab, kind, rows, scale, b.dO, loss);
+  ++g_launches;
+  const bf16* W[4];
+  for (int l = 0; l < 4; ++l) W[l] = wb + param_offset(l, false);
+  const int64_t kchunk = 4096;
+  // layer 4: dW4 = dO^T A3, db4 = sum dO, dA3 = dO W4
+  {
+    Epi e{grad + param_offset(3, false), kHidden, nullptr, 0, nullptr, 0, nullptr, 0, 1};
+    rc = gemm<true, false>(b.dO, kOutPad, b.A[2], kHidden, kOutPad, kHidden, rows, e, s, kchunk);
+    if (rc) return rc;
+    bias_grad_kernel<<<kOutPad, 256, 0, s>>>(b.dO, rows, kOutPad, grad + param_offset(3, true));
+    ++g_launches;
+    Epi d{b.dA, kHidden, nullptr, 0, nullptr, 0, nullptr, 0, 0};
+    rc = gemm<false, false>(b.dO, kOutPad, W[3], kHidden, rows, kHidden, kOutPad, d, s);
+    if (rc) return rc;
+  }
+  for (int l = 2; l >= 0; --l) {
+    gelu_back_kernel<<<grid1(rows * kHidden), 256, 0, s>>>(b.dA, b.Z[l], rows * kHidden, b.dZ);
+    ++g_launches;
+    const bf16* prev = l > 0 ? b.A[l - 1] : X;
+    const int kin = l > 0 ? kHidden : kIn;
+    Epi e{grad + param_offset(l, false), kin, nullptr, 0, nullptr, 0, nullptr, 0, 1};
+    rc = gemm<true, false>(b.dZ, kHidden, prev, kin, kHidden, kin, rows, e, s, kchunk);
+    if (rc) return rc;
+    bias_grad_kernel<<<kHidden, 256, 0, s>>>(b.dZ, rows, kHidden, grad + param_offset(l, true));
+    ++g_launches;
+    if (l > 0) {
+      Epi d{b.dA, kHidden, nullptr, 0, nullptr, 0, nullptr, 0, 0};
+      rc = gemm<false, false>(b.dZ, kHidden, W[l], kin, rows, kin, kHidden, d, s);
+      if (rc) return rc;
+    }
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(QBC_E_CUDA, "mlp gradient: %s", cudaGetErrorString(e));
+  return QBC_OK;
+}
+
+int Net::adam(float lr, cudaStream_t s) {
+  ++step_count;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.0f - std::pow(b1, (float)step_count), c2 = 1.0f - std::pow(b2, (float)step_count);
+  const int64_t n = param_count();
+  adam_kernel<<<grid1(n), 256, 0, s>>>(master, grad, m, v, n, lr, b1, b2, 1e-8f, c1, c2);
+  ++g_launches;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(QBC_E_CUDA, "mlp adam: %s", cudaGetErrorString(e));
+  return sync_weights(s);
+}
+
+}  // namespace mlp
+}  // namespace qbc

@@ -231,6 +231,51 @@ class OctreeGLC:
                                        int(n), b.ctypes.data_as(_lib.c_float_p), b.shape[0], C.c_void_p(out_pts),
                                        C.c_void_p(out_nrm)))
 
+    # ---- occluder-proposal network ----
+    def proposal_collect(self, views: Sequence[View]) -> int:
+        n = len(views)
+        varr = (View * n)(*views)
+        cnt = C.c_int64()
+        check(self._lib.qbc_proposal_collect(self.handle, varr, n, C.byref(cnt)))
+        return cnt.value
+
+    def proposal_train(self, steps: int, batch: int = 4096, lr: float = 2e-3, seed: int = 1) -> dict:
+        st = _lib.TrainStats()
+        check(self._lib.qbc_proposal_train(self.handle, C.byref(_lib.TrainOpts(int(steps), int(batch), float(lr), 0,
+                                                                               int(seed))), C.byref(st)))
+        return st.as_dict()
+
+    def proposal_clear(self) -> None:
+        check(self._lib.qbc_proposal_clear(self.handle))
+
+    def proposal_params(self) -> np.ndarray:
+        out = np.zeros(_lib.PROPOSAL_PARAMS, np.float32)
+        check(self._lib.qbc_proposal_get_params(self.handle, out.ctypes.data_as(_lib.c_float_p)))
+        return out
+
+    def proposal_set_params(self, params: np.ndarray) -> None:
+        p = np.ascontiguousarray(params, np.float32)
+        assert p.size == _lib.PROPOSAL_PARAMS
+        check(self._lib.qbc_proposal_set_params(self.handle, p.ctypes.data_as(_lib.c_float_p)))
+
+    def proposal_eval(self, x: np.ndarray) -> np.ndarray:
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, 45)
+        out = np.zeros((x.shape[0], 4), np.float32)
+        check(self._lib.qbc_proposal_eval(self.handle, x.ctypes.data_as(_lib.c_float_p), x.shape[0],
+                                          out.ctypes.data_as(_lib.c_float_p)))
+        return out
+
+    def proposal_gradient(self, x: np.ndarray, t: np.ndarray, kind: np.ndarray):
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, 45)
+        t = np.ascontiguousarray(t, np.float32)
+        k = np.ascontiguousarray(kind, np.int8)
+        loss = C.c_float()
+        grad = np.zeros(_lib.PROPOSAL_PARAMS, np.float32)
+        check(self._lib.qbc_proposal_gradient(self.handle, x.ctypes.data_as(_lib.c_float_p),
+                                              t.ctypes.data_as(_lib.c_float_p), k.ctypes.data_as(C.POINTER(C.c_int8)),
+                                              x.shape[0], C.byref(loss), grad.ctypes.data_as(_lib.c_float_p)))
+        return loss.value, grad
+
     def set_option(self, option: int, value: int) -> None:
         check(self._lib.qbc_set_option(self.handle, int(option), int(value)))
 

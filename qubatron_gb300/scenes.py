@@ -173,6 +173,8 @@ class Workload:
     fov_deg: float = 60.0
     sizes: List = None        # per-view (width, height) when views differ in size
     character: int = 0        # points of a dynamic character re-skinned every frame
+    train_poses: List = None  # poses whose plain shadow walks train the occluder-proposal network
+    train_size: tuple = (320, 240)
 
 
 def aim(pos, target):
@@ -206,6 +208,18 @@ WORKLOADS = {
 _b64_sizes, _b64_poses = batch_views(64, 64)
 WORKLOADS["floor1m_char2m_mixed_x64"] = Workload("floor1m_char2m_mixed_x64", "floor1m", 0, 0, _b64_poses,
                                                  sizes=_b64_sizes, character=2_000_000)
+# learned occluder proposal on the floor scene: 256 training poses at 320x240
+# (about 10^7 logged shadow rays), 16 held-out poses at 1920x1080
+WORKLOADS["floor1m_mlp_1920x1080x16"] = Workload("floor1m_mlp_1920x1080x16", "floor1m", 1920, 1080,
+                                                 batch_views(3002, 16)[1], train_poses=batch_views(3001, 256)[1])
+
+
+def train_views(w: Workload, maxlevel: int = LEVELS, basesize: float = BASESIZE):
+    """qbc_view per training pose of a workload (empty if it has none)."""
+    from .octree_glc import view_setup
+    tw, th = w.train_size
+    return [view_setup(tw, th, pos, ang, w.lighta, w.quality, maxlevel, basesize, 0,
+                       vertical_fov_focal(th, w.fov_deg) if w.fov_deg else 0.0) for pos, ang in (w.train_poses or [])]
 
 
 def workload_views(w: Workload, maxlevel: int = LEVELS, basesize: float = BASESIZE):
