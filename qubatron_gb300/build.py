@@ -18,7 +18,7 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libqbcuda.so")
 
 SOURCES = ["qbcuda.cu", "build.cu", "mlp.cu", "host.cpp"]
-HEADERS = ["trace.cuh", "walker.cuh", "render.cuh", "qbc_internal.h", "mlp.h"]
+HEADERS = ["trace.cuh", "walker.cuh", "render.cuh", "qbc_internal.h", "mlp.h", "mlp_device.cuh"]
 
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "mlp.h"
+#include "mlp_device.cuh"
 #include "qbc_internal.h"
 
 using qbc::fail;
@@ -51,29 +52,10 @@ struct Epi {
   int atomic;
 };
 
-__device__ __forceinline__ float gelu_f(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
 __device__ __forceinline__ float gelu_grad(float x) {
   const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
   const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
   return cdf + x * pdf;
-}
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void ldsm_x4(uint32_t addr, uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3) {
-  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-               : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-               : "r"(addr));
-}
-
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-      "{%0,%1,%2,%3};\n"
-      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
 // C[M x N] = op(A)[M x K] * op(B)[K x N]. A is M x K row-major (TA false) or
@@ -98,14 +80,20 @@ __global__ void __launch_bounds__(128) gemm_kernel(const bf16* __restrict__ A, i
   const bf16 zero = __float2bfloat16(0.0f);
 
   for (int k0 = kb; k0 < ke; k0 += kKs) {
-    // stage op(A)[m0.., k0..] as As[m][k] and op(B)[k0.., n0..] as Bs[n][k]
+    // stage op(A)[m0.., k0..] as As[m][k] and op(B)[k0.., n0..] as Bs[n][k],
+    // consecutive threads along each operand's contiguous dimension
     for (int e = tid; e < kTile * kKs; e += 128) {
-      const int r = e / kKs, c = e % kKs;  // r: m or n, c: k
-      const int m = m0 + r, n = n0 + r, k = k0 + c;
-      bf16 a = zero, b = zero;
+      const int r = TA ? e % kTile : e / kKs, c = TA ? e / kTile : e % kKs;  // r: m, c: k
+      const int m = m0 + r, k = k0 + c;
+      bf16 a = zero;
       if (m < M && k < ke) a = TA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k];
-      if (n < N && k < ke) b = TB ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n];
       As[r][c] = a;
+    }
+    for (int e = tid; e < kTile * kKs; e += 128) {
+      const int r = TB ? e / kKs : e % kTile, c = TB ? e % kKs : e / kTile;  // r: n, c: k
+      const int n = n0 + r, k = k0 + c;
+      bf16 b = zero;
+      if (n < N && k < ke) b = TB ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n];
       Bs[r][c] = b;
     }
     __syncthreads();

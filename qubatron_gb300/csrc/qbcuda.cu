@@ -10,11 +10,13 @@
 #include <cstdint>
 #include <cstring>
 #include <mutex>
+#include <memory>
 #include <vector>
 
 #include "qbc_internal.h"
 #include "qbcuda.h"
 #include "mlp.h"
+#include "mlp_device.cuh"
 #include "render.cuh"
 
 using qbc::fail;
@@ -85,9 +87,7 @@ struct qbc_ctx {
   int8_t* ds_kind = nullptr;      // 1 occluded, 0 lit
   int64_t ds_cap = 0;
   unsigned int* ds_count = nullptr;
-  __nv_bfloat16* mq_x = nullptr;  // features of the queued records (inference)
-  float* mq_out = nullptr;
-  int64_t mq_cap = 0;
+  bool fused_attr[2] = {false, false};  // dynamic shared memory set for the fused network kernels
   int render_blocks[4] = {0, 0, 0, 0};  // resident blocks per SM of each render_kernel variant
   int attr_done = 0;
   int service_min = qbc::kServiceMinDefault;
@@ -203,8 +203,6 @@ extern "C" int qbc_destroy(qbc_ctx* c) {
   cudaFree(c->ds_t);
   cudaFree(c->ds_kind);
   cudaFree(c->ds_count);
-  cudaFree(c->mq_x);
-  cudaFree(c->mq_out);
   cudaFree(c->rec);
   cudaFree(c->wcount);
   cudaFree(c->wstats);
@@ -618,31 +616,58 @@ __global__ void collect_kernel(const __grid_constant__ qbc::Batch b, const __gri
   }
 }
 
-__global__ void record_features_kernel(const __grid_constant__ qbc::Batch b, const __grid_constant__ qbc::Wave w,
-                                       unsigned total, bf16* __restrict__ X) {
-  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x)
-    record_features(b, w.rec + (size_t)q * qbc::kRecWords, X + (size_t)q * qbc::mlp::kIn);
-}
-
-// Network outputs -> the records' proposals, earliest first; none where
-// the occlusion logit is below the gate.
-__global__ void write_proposals_kernel(const __grid_constant__ qbc::Wave w, unsigned total,
-                                       const float* __restrict__ out, float gate) {
-  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
-    const float* o = out + (size_t)q * qbc::mlp::kOutPad;
+// Fused-network rows over the shade-pass record queue: the features of each
+// record in, its proposals out (earliest first; none where the occlusion
+// logit is below the gate). The row count is read on the device.
+struct RecordRows {
+  qbc::Batch b;
+  qbc::Wave w;
+  float gate;
+  __device__ __forceinline__ uint32_t rows() const { return min(*w.qcount, w.cap); }
+  __device__ __forceinline__ void load(uint32_t r0, uint32_t n, bf16* x, int lane) const {
+    if (lane >= 16) return;
+    bf16* row = x + lane * qbc::mlp::kLdIn;
+    if ((uint32_t)lane < n) {
+      record_features(b, w.rec + (size_t)(r0 + lane) * qbc::kRecWords, row);
+    } else {
+      for (int k = 0; k < qbc::mlp::kIn; ++k) row[k] = __float2bfloat16(0.0f);
+    }
+  }
+  __device__ __forceinline__ void store(uint32_t r, const float* o) const {
     float t[3] = {o[0], o[1], o[2]};
     if (!(o[qbc::mlp::kGate] >= gate)) t[0] = t[1] = t[2] = -1.0f;
     for (int i = 0; i < 2; ++i)
       for (int j = i + 1; j < 3; ++j)
         if (t[j] < t[i]) {
-          float x = t[i];
+          const float x = t[i];
           t[i] = t[j];
           t[j] = x;
         }
-    uint32_t* r = w.rec + (size_t)q * qbc::kRecWords;
-    for (int k = 0; k < 3; ++k) r[qbc::kRecProp + k] = __float_as_uint(t[k]);
+    uint32_t* rec = w.rec + (size_t)r * qbc::kRecWords;
+    for (int k = 0; k < 3; ++k) rec[qbc::kRecProp + k] = __float_as_uint(t[k]);
   }
-}
+};
+
+// Fused-network rows over a bf16 feature matrix (kIn per row) -> kOutUsed
+// floats per row.
+struct MatrixRows {
+  const bf16* X;
+  float* out;
+  uint32_t m;
+  __device__ __forceinline__ uint32_t rows() const { return m; }
+  __device__ __forceinline__ void load(uint32_t r0, uint32_t n, bf16* x, int lane) const {
+    constexpr int kVec = qbc::mlp::kIn / 8;
+    for (int e = lane; e < 16 * kVec; e += 32) {
+      const int r = e / kVec, c = e % kVec;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if ((uint32_t)r < n) v = reinterpret_cast<const uint4*>(X + (size_t)(r0 + r) * qbc::mlp::kIn)[c];
+      *reinterpret_cast<uint4*>(x + r * qbc::mlp::kLdIn + c * 8) = v;
+    }
+  }
+  __device__ __forceinline__ void store(uint32_t r, const float* o) const {
+    for (int k = 0; k < qbc::mlp::kOutUsed; ++k) out[(size_t)r * qbc::mlp::kOutUsed + k] = o[k];
+  }
+};
 
 // Random minibatch of the training set.
 __global__ void gather_kernel(const bf16* __restrict__ X, const float* __restrict__ tl,
@@ -669,34 +694,41 @@ bf16 host_bf16(float f) {
   return __ushort_as_bfloat16((unsigned short)(u >> 16));
 }
 
+// One launch of the fused network over `src`'s rows: a persistent grid of
+// resident blocks, each staging the weights once.
+template <class Src>
+int launch_fused(qbc_ctx* c, const Src& src, int variant) {
+  using qbc::mlp::FusedSmem;
+  auto kern = qbc::mlp::fused_forward_kernel<Src>;
+  if (!c->fused_attr[variant]) {
+    QBC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FusedSmem)));
+    c->fused_attr[variant] = true;
+  }
+  int per_sm = 0;
+  QBC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, qbc::mlp::kFusedThreads, sizeof(FusedSmem)));
+  if (per_sm < 1) return fail(QBC_E_STATE, "proposal network: no block fits on an SM");
+  qbc::mlp::FusedParams p;
+  for (int l = 0; l < 4; ++l) {
+    p.w[l] = c->net.wb + qbc::mlp::param_offset(l, false);
+    p.b[l] = c->net.master + qbc::mlp::param_offset(l, true);
+    if (reinterpret_cast<uintptr_t>(p.w[l]) % 16) return fail(QBC_E_STATE, "proposal network: unaligned weights");
+  }
+  kern<<<per_sm * c->sm_count, qbc::mlp::kFusedThreads, sizeof(FusedSmem), c->stream>>>(p, src);
+  QBC_CUDA(cudaGetLastError());
+  ++c->launches;
+  return QBC_OK;
+}
+
+// Proposals of every queued record from the network (no host round trip:
+// the kernel reads the queue length on the device).
 int propose_mlp(qbc_ctx* c, const qbc::Batch& b, const qbc::Wave& w) {
   if (!c->net.ready) return fail(QBC_E_STATE, "qbc_render_views_ex: no occluder network in this context");
-  unsigned total = 0;
-  QBC_CUDA(cudaMemcpyAsync(&total, w.qcount, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
-  QBC_CUDA(cudaStreamSynchronize(c->stream));
-  total = std::min(total, w.cap);
-  if (total == 0) return QBC_OK;
-  if (c->mq_cap < total) {
-    int64_t cap = (int64_t)total + total / 4;
-    int rc = grow(&c->mq_x, &c->mq_cap, cap, (size_t)qbc::mlp::kIn * 2, "proposal features");
-    if (rc) return rc;
-    cudaFree(c->mq_out);
-    c->mq_out = nullptr;
-    cudaError_t e = cudaMalloc(&c->mq_out, (size_t)cap * qbc::mlp::kOutPad * 4);
-    if (e != cudaSuccess) return fail(QBC_E_NOMEM, "proposal outputs: %s", cudaGetErrorString(e));
-  }
-  record_features_kernel<<<launch_grid(c, total), 256, 0, c->stream>>>(b, w, total, c->mq_x);
-  QBC_CUDA(cudaGetLastError());
-  const int64_t l0 = qbc::mlp::launches();
-  int rc = c->net.forward(c->mq_x, total, c->mq_out, c->stream);
-  c->launches += qbc::mlp::launches() - l0;
-  if (rc) return rc;
+  std::unique_ptr<RecordRows> src(new RecordRows());
+  src->b = b;
+  src->w = w;
   const float p = (float)c->proposal_gate * 1e-3f;  // gate probability -> logit
-  const float gate = c->proposal_gate <= 0 ? -INFINITY : logf(p / (1.0f - p));
-  write_proposals_kernel<<<launch_grid(c, total), 256, 0, c->stream>>>(w, total, c->mq_out, gate);
-  QBC_CUDA(cudaGetLastError());
-  c->launches += 2;
-  return QBC_OK;
+  src->gate = c->proposal_gate <= 0 ? -INFINITY : logf(p / (1.0f - p));
+  return launch_fused(c, *src, 0);
 }
 
 int ensure_dataset(qbc_ctx* c, int64_t cap) {
@@ -1359,7 +1391,8 @@ extern "C" int qbc_proposal_set_params(qbc_ctx* c, const float* params) {
 
 extern "C" int qbc_proposal_eval(qbc_ctx* c, const float* x, int64_t m, float* out) {
   qbc::clear_error();
-  if (!c || (m > 0 && (!x || !out)) || m < 0) return fail(QBC_E_ARG, "qbc_proposal_eval: bad argument");
+  if (!c || (m > 0 && (!x || !out)) || m < 0 || m > (1ll << 31))
+    return fail(QBC_E_ARG, "qbc_proposal_eval: bad argument");
   if (!c->net.ready) return fail(QBC_E_STATE, "qbc_proposal_eval: no network");
   if (m == 0) return QBC_OK;
   QBC_CUDA(cudaSetDevice(c->device));
@@ -1367,25 +1400,21 @@ extern "C" int qbc_proposal_eval(qbc_ctx* c, const float* x, int64_t m, float* o
   int rc = upload_features(c, x, m, &dx);
   if (rc) return rc;
   float* dout = nullptr;
-  cudaError_t e = cudaMalloc(&dout, (size_t)m * qbc::mlp::kOutPad * 4);
+  cudaError_t e = cudaMalloc(&dout, (size_t)m * qbc::mlp::kOutUsed * 4);
   if (e != cudaSuccess) {
     cudaFree(dx);
     return fail(QBC_E_NOMEM, "qbc_proposal_eval: %s", cudaGetErrorString(e));
   }
-  rc = c->net.forward(dx, m, dout, c->stream);
-  std::vector<float> h((size_t)m * qbc::mlp::kOutPad);
+  MatrixRows src{dx, dout, (uint32_t)m};
+  rc = launch_fused(c, src, 1);
   if (!rc) {
-    e = cudaMemcpyAsync(h.data(), dout, h.size() * 4, cudaMemcpyDeviceToHost, c->stream);
+    e = cudaMemcpyAsync(out, dout, (size_t)m * qbc::mlp::kOutUsed * 4, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) rc = fail(QBC_E_CUDA, "qbc_proposal_eval: %s", cudaGetErrorString(e));
   }
   cudaFree(dx);
   cudaFree(dout);
-  if (rc) return rc;
-  for (int64_t i = 0; i < m; ++i)
-    for (int k = 0; k < qbc::mlp::kOutUsed; ++k)
-      out[i * qbc::mlp::kOutUsed + k] = h[(size_t)i * qbc::mlp::kOutPad + k];
-  return QBC_OK;
+  return rc;
 }
 
 extern "C" int qbc_proposal_gradient(qbc_ctx* c, const float* x, const float* t, const int8_t* kind, int64_t m,

@@ -174,7 +174,7 @@ class Workload:
     sizes: List = None        # per-view (width, height) when views differ in size
     character: int = 0        # points of a dynamic character re-skinned every frame
     train_poses: List = None  # poses whose plain shadow walks train the occluder-proposal network
-    train_size: tuple = (320, 240)
+    train_size: tuple = (960, 720)
 
 
 def aim(pos, target):
@@ -208,7 +208,7 @@ WORKLOADS = {
 _b64_sizes, _b64_poses = batch_views(64, 64)
 WORKLOADS["floor1m_char2m_mixed_x64"] = Workload("floor1m_char2m_mixed_x64", "floor1m", 0, 0, _b64_poses,
                                                  sizes=_b64_sizes, character=2_000_000)
-# learned occluder proposal on the floor scene: 256 training poses at 320x240
+# learned occluder proposal on the floor scene: 256 training poses at 960x720
 # (about 10^7 logged shadow rays), 16 held-out poses at 1920x1080
 WORKLOADS["floor1m_mlp_1920x1080x16"] = Workload("floor1m_mlp_1920x1080x16", "floor1m", 1920, 1080,
                                                  batch_views(3002, 16)[1], train_poses=batch_views(3001, 256)[1])
