@@ -291,6 +291,28 @@ typedef struct qbc_render_stats
 int qbc_render_views_ex(qbc_ctx* ctx, const qbc_view* views, const qbc_outputs* outs, int n, int outputs_on_device, const qbc_render_opts* opts, qbc_render_stats* stats);
 
 /*
+ * A frame as a CUDA graph (not part of the reference: the GL connector
+ * redraws through the driver each frame). qbc_graph_capture renders the
+ * views once into the device outputs, then captures the same frame (every
+ * memset and kernel qbc_render_views_ex enqueues with these options) on the
+ * context's stream as a CUDA graph and instantiates it. qbc_graph_launch
+ * replays the frame with one launch call on the context's stream;
+ * qbc_graph_update re-captures it for new uniforms of the same view sizes
+ * (camera, light, quality) and updates the instantiated graph in place.
+ * The graph holds the device addresses and sizes of the trees, models and
+ * work buffers, the stream and the tuning options as they were at capture:
+ * after an upload, build, qbc_set_stream or qbc_set_option that changes any
+ * of them, qbc_graph_launch fails with QBC_E_STATE until qbc_graph_update.
+ * Render statistics are not collected. qbc_destroy detaches the context's
+ * graphs: afterwards they only accept qbc_graph_destroy.
+ */
+typedef struct qbc_graph qbc_graph;
+int qbc_graph_capture(qbc_ctx* ctx, const qbc_view* views, const qbc_outputs* dev_outs, int n, const qbc_render_opts* opts, qbc_graph** graph);
+int qbc_graph_update(qbc_graph* graph, const qbc_view* views, int n);
+int qbc_graph_launch(qbc_graph* graph);
+int qbc_graph_destroy(qbc_graph* graph);
+
+/*
  * Occluder-proposal network (QBC_PROPOSE_MLP; not part of the reference).
  * A 45 -> 128 -> 128 -> 128 -> 4 GELU network, BF16 weights and activations
  * on the tensor cores with FP32 accumulation, trained on the GPU. Input of a

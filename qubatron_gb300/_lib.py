@@ -189,6 +189,11 @@ SIGNATURES = {
     "qbc_render_views_ex": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int, C.c_int,
                                       C.POINTER(RenderOpts), C.POINTER(RenderStats)]),
     "qbc_render_views_noalloc": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int]),
+    "qbc_graph_capture": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int, C.POINTER(RenderOpts),
+                                    C.POINTER(C.c_void_p)]),
+    "qbc_graph_update": (C.c_int, [C.c_void_p, C.POINTER(View), C.c_int]),
+    "qbc_graph_launch": (C.c_int, [C.c_void_p]),
+    "qbc_graph_destroy": (C.c_int, [C.c_void_p]),
     "qbc_proposal_collect": (C.c_int, [C.c_void_p, C.POINTER(View), C.c_int, c_int64_p]),
     "qbc_proposal_train": (C.c_int, [C.c_void_p, C.POINTER(TrainOpts), C.POINTER(TrainStats)]),
     "qbc_proposal_clear": (C.c_int, [C.c_void_p]),

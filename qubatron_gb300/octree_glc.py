@@ -151,6 +151,17 @@ class OctreeGLC:
         stats = self.render_views_ex(views, [b.outputs() for b in bufs], False, **kw)
         return bufs, stats
 
+    def graph_capture(self, views: Sequence[View], outputs: Sequence[Outputs], two_pass: bool = False,
+                      proposals: int = 0, proposal_level: int = 0, seed: int = 0) -> "FrameGraph":
+        """qbc_graph_capture: the frame (device outputs) as a CUDA graph."""
+        n = len(views)
+        varr = (View * n)(*views)
+        oarr = (Outputs * n)(*outputs)
+        opts = _lib.RenderOpts(int(two_pass), int(proposals), 0, int(proposal_level), int(seed))
+        h = C.c_void_p()
+        check(self._lib.qbc_graph_capture(self.handle, varr, oarr, n, C.byref(opts), C.byref(h)))
+        return FrameGraph(self, h, n)
+
     def render_views_noalloc(self, views: Sequence[View], outputs: Sequence[Outputs]) -> None:
         """qbc_render_views_noalloc: device outputs only, no allocation in
         the call (the work-queue counters live in static device memory)."""
@@ -333,3 +344,39 @@ def octree_glc_upload_texbuffer_data(rc: OctreeGLC, data, type: int, size: int, 
 def octree_glc_update(rc: OctreeGLC, width: float, height: float, position, angle, lighta: float, quality: int,
                       maxlevel: int, basesize: float, shoot: int = 0) -> np.ndarray:
     return rc.update(width, height, position, angle, lighta, quality, maxlevel, basesize, shoot)
+
+
+class FrameGraph:
+    """qbc_graph: a captured frame; launch() replays it, update(views)
+    re-captures it for new uniforms of the same view sizes."""
+
+    def __init__(self, owner: OctreeGLC, handle: C.c_void_p, n: int):
+        self._owner = owner  # the context outlives the graph
+        self._lib = owner._lib
+        self.handle = handle
+        self.n = n
+
+    def launch(self) -> None:
+        check(self._lib.qbc_graph_launch(self.handle))
+
+    def update(self, views: Sequence[View]) -> None:
+        n = len(views)
+        varr = (View * n)(*views)
+        check(self._lib.qbc_graph_update(self.handle, varr, n))
+
+    def close(self) -> None:
+        if self.handle:
+            self._lib.qbc_graph_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
