@@ -300,8 +300,19 @@ def run_gpu(args):
     def render_two_pass(v, o, dev):
         ctx.render_views_ex(v, o, dev, two_pass=True)
 
+    mlp_kw = dict(two_pass=True, proposals=qb._lib.PROPOSE_MLP, proposal_level=args.proposal_level)
+
     def render_mlp(v, o, dev):
-        ctx.render_views_ex(v, o, dev, two_pass=True, proposals=qb._lib.PROPOSE_MLP, proposal_level=args.proposal_level)
+        ctx.render_views_ex(v, o, dev, **mlp_kw)
+
+    graphs = []
+
+    def as_graph(kw):
+        """The frame as a CUDA graph (static scenes): each step is one
+        qbc_graph_launch into the device outputs."""
+        g = ctx.graph_capture(views, outs, **kw)
+        graphs.append(g)
+        return lambda v, o, dev: g.launch()
 
     render = render_plain
     training = None
@@ -342,6 +353,18 @@ def run_gpu(args):
     def update(frame):
         if chars:
             chars.apply(poses[frame])
+
+    tuning = None
+    if args.autotune and not args.service_min:
+        # tuning options (service threshold, warp tile, blocks per SM) picked
+        # by timing this frame; untimed
+        update(0)
+        tuning = ctx.autotune(views, outs, reps=3, **(mlp_kw if training is not None else {}))
+        torch.cuda.synchronize()
+
+    use_graph = args.graph and chars is None
+    if use_graph:
+        render = as_graph(mlp_kw if training is not None else {})
 
     # untimed instrumented passes: rays cast and node visits of every timed
     # frame (a static scene needs one)
@@ -411,8 +434,8 @@ def run_gpu(args):
     if training is not None:
         # the same frames without the network (fused kernel, and the same
         # two-pass pipeline), and the proposal statistics of one frame
-        plain_ms, _, _ = timed(render_plain)
-        two_ms, _, _ = timed(render_two_pass)
+        plain_ms, _, _ = timed(as_graph({}) if use_graph else render_plain)
+        two_ms, _, _ = timed(as_graph({"two_pass": True}) if use_graph else render_two_pass)
         st_mlp = ctx.render_views_ex(views, outs, True, two_pass=True, proposals=qb._lib.PROPOSE_MLP,
                                      proposal_level=args.proposal_level)
         st_two = ctx.render_views_ex(views, outs, True, two_pass=True)
@@ -444,7 +467,8 @@ def run_gpu(args):
     e2e = None
     if not args.no_e2e:
         e2e = measure_e2e(ctx, views, rays, world, flush, args.steps,
-                          (lambda k: update(args.warmup + k % args.steps)) if chars else None, render)
+                          (lambda k: update(args.warmup + k % args.steps)) if chars else None,
+                          render_mlp if training is not None else render_plain)
 
     hbm, peak_kind = peaks()
 
@@ -482,6 +506,10 @@ def run_gpu(args):
     if proposal is not None:
         line["config"]["per_step"] = "two-pass render with occluder-network proposals (network evaluated every step)"
         line["proposal"] = proposal
+    line["config"]["launch"] = "CUDA graph replay (qbc_graph_launch)" if use_graph else "eager (qbc_render_views*)"
+    line["config"]["tuning"] = tuning
+    for g in graphs:
+        g.close()
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_sample(scene, views, budget_s=args.cpu_seconds,
                                                             character=character, frame=args.warmup).items()
@@ -506,6 +534,10 @@ def main():
     ap.add_argument("--service-min", type=int, default=0, help="override the kernel's service threshold")
     ap.add_argument("--workload", default=None)
     ap.add_argument("--train-steps", type=int, default=4000, help="occluder-network training steps")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="keep the default tuning options instead of autotuning them on the frame")
+    ap.add_argument("--no-graph", dest="graph", action="store_false",
+                    help="time eager launches instead of CUDA graph replays of the frame")
     ap.add_argument("--proposal-gate", type=int, default=500, help="occlusion probability (per mille) to try")
     ap.add_argument("--proposal-level", type=int, default=8, help="octree level of the proposed cells")
     args = ap.parse_args()

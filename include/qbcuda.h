@@ -291,6 +291,29 @@ typedef struct qbc_render_stats
 int qbc_render_views_ex(qbc_ctx* ctx, const qbc_view* views, const qbc_outputs* outs, int n, int outputs_on_device, const qbc_render_opts* opts, qbc_render_stats* stats);
 
 /*
+ * Autotuner (not part of the reference). Times frames of these views
+ * (device outputs, these render options) on the context's stream under
+ * candidate tuning options, one option after another with the others kept
+ * at their best so far: the service threshold (1..16), the warp tile width
+ * (4, 8, 16, 32) and the render blocks per SM (0, 2..8). Each candidate gets
+ * one untimed frame, then `reps` (1..101) frames timed with CUDA events; its
+ * time is their median. The fastest setting stays set on the context (the
+ * initial one on error). The options change only the time of a frame, never
+ * its pixels.
+ */
+typedef struct qbc_tune_result
+{
+    int32_t tile_width;
+    int32_t blocks_per_sm;
+    int32_t service_min;
+    int32_t candidates;  /* settings timed */
+    float   ms_initial;  /* median frame time under the options found */
+    float   ms_best;     /* ... under the options left set */
+} qbc_tune_result;
+
+int qbc_autotune(qbc_ctx* ctx, const qbc_view* views, const qbc_outputs* dev_outs, int n, const qbc_render_opts* opts, int reps, qbc_tune_result* result);
+
+/*
  * A frame as a CUDA graph (not part of the reference: the GL connector
  * redraws through the driver each frame). qbc_graph_capture renders the
  * views once into the device outputs, then captures the same frame (every
@@ -374,9 +397,15 @@ int qbc_synchronize(qbc_ctx* ctx);
  *   QBC_OPT_PROPOSAL_GATE  0..999 per mille, default 500: QBC_PROPOSE_MLP
  *   tries a pixel's proposals only when the network's occlusion probability
  *   is at least this (0: always).
+ *   QBC_OPT_TILE_WIDTH  4, 8 (default), 16 or 32: width of the 32-pixel warp
+ *   tiles the render kernels take from their queue (height 32 / width).
+ *   QBC_OPT_BLOCKS_PER_SM  0 (default: as many as fit) .. 32: resident
+ *   render blocks per SM of the persistent grid.
  */
 #define QBC_OPT_SERVICE_MIN 1
 #define QBC_OPT_PROPOSAL_GATE 2
+#define QBC_OPT_TILE_WIDTH 3
+#define QBC_OPT_BLOCKS_PER_SM 4
 int qbc_set_option(qbc_ctx* ctx, int option, int value);
 int qbc_get_option(qbc_ctx* ctx, int option, int* value);
 

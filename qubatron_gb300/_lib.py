@@ -132,6 +132,16 @@ PROPOSE_NONE, PROPOSE_MLP, PROPOSE_LOGGED, PROPOSE_RANDOM = 0, 1, 2, 3
 PROPOSAL_PARAMS = 41360
 
 
+class TuneResult(C.Structure):
+    """qbc_tune_result."""
+
+    _fields_ = [("tile_width", C.c_int32), ("blocks_per_sm", C.c_int32), ("service_min", C.c_int32),
+                ("candidates", C.c_int32), ("ms_initial", C.c_float), ("ms_best", C.c_float)]
+
+    def as_dict(self) -> dict:
+        return {f: (float(getattr(self, f)) if f.startswith("ms") else int(getattr(self, f))) for f, _ in self._fields_}
+
+
 class TrainOpts(C.Structure):
     """qbc_train_opts."""
 
@@ -189,6 +199,8 @@ SIGNATURES = {
     "qbc_render_views_ex": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int, C.c_int,
                                       C.POINTER(RenderOpts), C.POINTER(RenderStats)]),
     "qbc_render_views_noalloc": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int]),
+    "qbc_autotune": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int, C.POINTER(RenderOpts), C.c_int,
+                               C.POINTER(TuneResult)]),
     "qbc_graph_capture": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int, C.POINTER(RenderOpts),
                                     C.POINTER(C.c_void_p)]),
     "qbc_graph_update": (C.c_int, [C.c_void_p, C.POINTER(View), C.c_int]),
@@ -227,6 +239,8 @@ _LIB = None
 
 OPT_SERVICE_MIN = 1
 OPT_PROPOSAL_GATE = 2
+OPT_TILE_WIDTH = 3
+OPT_BLOCKS_PER_SM = 4
 
 
 def lib_path() -> str:

@@ -92,6 +92,8 @@ struct qbc_ctx {
   int render_blocks[4] = {0, 0, 0, 0};  // resident blocks per SM of each render_kernel variant
   int attr_done = 0;
   int service_min = qbc::kServiceMinDefault;
+  int tile_shift = 3;     // 8x4 warp tiles
+  int blocks_per_sm = 0;  // render blocks per SM (0: as many as fit)
   int proposal_gate = 500;  // per mille: minimum predicted occlusion probability to try a proposal
   int64_t launches = 0;
 };
@@ -234,6 +236,17 @@ extern "C" int qbc_set_option(qbc_ctx* c, int option, int value) {
     c->proposal_gate = value;
     return QBC_OK;
   }
+  if (option == QBC_OPT_TILE_WIDTH) {
+    if (value != 4 && value != 8 && value != 16 && value != 32)
+      return fail(QBC_E_ARG, "qbc_set_option: tile width %d (4, 8, 16 or 32)", value);
+    c->tile_shift = value == 4 ? 2 : value == 8 ? 3 : value == 16 ? 4 : 5;
+    return QBC_OK;
+  }
+  if (option == QBC_OPT_BLOCKS_PER_SM) {
+    if (value < 0 || value > 32) return fail(QBC_E_ARG, "qbc_set_option: blocks per SM %d outside 0..32", value);
+    c->blocks_per_sm = value;
+    return QBC_OK;
+  }
   return fail(QBC_E_ARG, "qbc_set_option: unknown option %d", option);
 }
 
@@ -245,6 +258,14 @@ extern "C" int qbc_get_option(qbc_ctx* c, int option, int* value) {
   }
   if (option == QBC_OPT_PROPOSAL_GATE) {
     *value = c->proposal_gate;
+    return QBC_OK;
+  }
+  if (option == QBC_OPT_TILE_WIDTH) {
+    *value = 1 << c->tile_shift;
+    return QBC_OK;
+  }
+  if (option == QBC_OPT_BLOCKS_PER_SM) {
+    *value = c->blocks_per_sm;
     return QBC_OK;
   }
   return fail(QBC_E_ARG, "qbc_get_option: unknown option %d", option);
@@ -834,6 +855,7 @@ int launch_render(qbc_ctx* c, const qbc::Batch& b, size_t smem, const qbc::Wave&
   QBC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, qbc::kThreads, smem));
   if (per_sm < 1) return fail(QBC_E_STATE, "render_kernel: no block fits on an SM with %zu B shared memory", smem);
   if (MODE == qbc::kFused && !PROP) c->render_blocks[(EXACT ? 1 : 0) + (DYN ? 2 : 0)] = per_sm;
+  if (c->blocks_per_sm > 0) per_sm = std::min(per_sm, c->blocks_per_sm);
   // persistent: one wave of resident blocks, never more blocks than warp tiles
   int64_t blocks = (int64_t)per_sm * c->sm_count;
   if (MODE != qbc::kShadePass) blocks = std::min<int64_t>(blocks, ((int64_t)b.tiles_total + 3) / 4);
@@ -904,8 +926,9 @@ int launch_batch(qbc_ctx* c, const qbc_view* views, const qbc_outputs* dev_outs,
     qbc::ViewJob& J = b->job[i];
     J.v = views[i];
     J.o = dev_outs[i];
-    J.tiles_x = (views[i].width_px + 7) / 8;
-    int tiles_y = (views[i].height_px + 3) / 4;
+    const int tw = 1 << c->tile_shift, th = 32 >> c->tile_shift;
+    J.tiles_x = (views[i].width_px + tw - 1) / tw;
+    int tiles_y = (views[i].height_px + th - 1) / th;
     J.tile_begin = tiles;
     J.pixel_begin = pixels;
     tiles += J.tiles_x * tiles_y;
@@ -917,6 +940,7 @@ int launch_batch(qbc_ctx* c, const qbc_view* views, const qbc_outputs* dev_outs,
   b->tiles_total = tiles;
   b->max_level = maxlevel;
   b->service_min = c->service_min;
+  b->tile_shift = c->tile_shift;
   const bool dyn = c->tree[1].n > 0;
   const size_t words = (size_t)(dyn ? 3 : 2) * maxlevel + qbc::kPixWords;
   const size_t smem = words * qbc::kThreads * sizeof(uint32_t);
@@ -1038,6 +1062,8 @@ struct FrameSignature {
   const void* stream;
   int32_t service_min;
   int32_t proposal_gate;
+  int32_t tile_shift;
+  int32_t blocks_per_sm;
 };
 
 bool same_signature(const FrameSignature& a, const FrameSignature& b) {
@@ -1049,7 +1075,7 @@ bool same_signature(const FrameSignature& a, const FrameSignature& b) {
   }
   return a.rec == b.rec && a.rec_cap == b.rec_cap && a.pixlog == b.pixlog && a.pixlog_cap == b.pixlog_cap &&
          a.net_w == b.net_w && a.net_b == b.net_b && a.stream == b.stream && a.service_min == b.service_min &&
-         a.proposal_gate == b.proposal_gate;
+         a.proposal_gate == b.proposal_gate && a.tile_shift == b.tile_shift && a.blocks_per_sm == b.blocks_per_sm;
 }
 
 FrameSignature frame_signature(const qbc_ctx* c) {
@@ -1064,6 +1090,8 @@ FrameSignature frame_signature(const qbc_ctx* c) {
   f.stream = c->stream;
   f.service_min = c->service_min;
   f.proposal_gate = c->proposal_gate;
+  f.tile_shift = c->tile_shift;
+  f.blocks_per_sm = c->blocks_per_sm;
   return f;
 }
 
@@ -1237,6 +1265,103 @@ extern "C" int qbc_graph_destroy(qbc_graph* g) {
   return QBC_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Autotuner: service threshold, warp tile width, render blocks per SM
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct TuneSetting {
+  int shift, blocks, service;
+};
+
+// Median device time of `reps` frames (after one untimed frame).
+int time_frames(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs, int n, const qbc_render_opts* opts,
+                int reps, cudaEvent_t* ev, float* ms) {
+  int rc = render_views_impl(c, views, outs, n, 1, opts, nullptr);
+  if (rc) return rc;
+  std::vector<float> t((size_t)reps);
+  for (int r = 0; r < reps; ++r) {
+    QBC_CUDA(cudaEventRecord(ev[0], c->stream));
+    rc = render_views_impl(c, views, outs, n, 1, opts, nullptr);
+    if (rc) return rc;
+    QBC_CUDA(cudaEventRecord(ev[1], c->stream));
+    QBC_CUDA(cudaEventSynchronize(ev[1]));
+    QBC_CUDA(cudaEventElapsedTime(&t[(size_t)r], ev[0], ev[1]));
+  }
+  std::sort(t.begin(), t.end());
+  *ms = t[(size_t)reps / 2];
+  return QBC_OK;
+}
+
+int autotune_impl(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs, int n, const qbc_render_opts* opts,
+                  int reps, cudaEvent_t* ev, TuneSetting* best, qbc_tune_result* res) {
+  auto apply = [c](const TuneSetting& s) {
+    c->tile_shift = s.shift;
+    c->blocks_per_sm = s.blocks;
+    c->service_min = s.service;
+  };
+  float best_ms = 0.0f;
+  int rc = time_frames(c, views, outs, n, opts, reps, ev, &best_ms);
+  if (rc) return rc;
+  res->ms_initial = best_ms;
+  res->candidates = 1;
+  auto consider = [&](const TuneSetting& s) -> int {
+    apply(s);
+    float ms = 0.0f;
+    int e = time_frames(c, views, outs, n, opts, reps, ev, &ms);
+    if (e) return e;
+    ++res->candidates;
+    if (ms < best_ms) {
+      best_ms = ms;
+      *best = s;
+    }
+    return QBC_OK;
+  };
+  // one option at a time, each kept at its best before the next is swept
+  for (int sm : {1, 2, 3, 4, 6, 8, 12, 16})
+    if (sm != best->service && (rc = consider({best->shift, best->blocks, sm}))) return rc;
+  for (int sh : {2, 3, 4, 5})
+    if (sh != best->shift && (rc = consider({sh, best->blocks, best->service}))) return rc;
+  for (int bl : {0, 2, 3, 4, 6, 8})
+    if (bl != best->blocks && (rc = consider({best->shift, bl, best->service}))) return rc;
+  res->ms_best = best_ms;
+  return QBC_OK;
+}
+
+}  // namespace
+
+extern "C" int qbc_autotune(qbc_ctx* c, const qbc_view* views, const qbc_outputs* dev_outs, int n,
+                            const qbc_render_opts* opts, int reps, qbc_tune_result* result) {
+  qbc::clear_error();
+  if (!c || !views || !dev_outs || !result || n <= 0) return fail(QBC_E_ARG, "qbc_autotune: bad argument");
+  if (reps < 1 || reps > 101) return fail(QBC_E_ARG, "qbc_autotune: reps %d outside 1..101", reps);
+  int rc = check_render_opts(opts, n);
+  if (rc) return rc;
+  QBC_CUDA(cudaSetDevice(c->device));
+  std::memset(result, 0, sizeof(*result));
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  QBC_CUDA(cudaEventCreate(&ev[0]));
+  if (cudaEventCreate(&ev[1]) != cudaSuccess) {
+    cudaEventDestroy(ev[0]);
+    return fail(QBC_E_CUDA, "qbc_autotune: event");
+  }
+  const TuneSetting initial{c->tile_shift, c->blocks_per_sm, c->service_min};
+  TuneSetting best = initial;
+  rc = autotune_impl(c, views, dev_outs, n, opts, reps, ev, &best, result);
+  const TuneSetting keep = rc ? initial : best;
+  c->tile_shift = keep.shift;
+  c->blocks_per_sm = keep.blocks;
+  c->service_min = keep.service;
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  if (rc) return rc;
+  result->tile_width = 1 << keep.shift;
+  result->blocks_per_sm = keep.blocks;
+  result->service_min = keep.service;
+  return QBC_OK;
+}
+
 extern "C" int qbc_trace_rays(qbc_ctx* c, const float* pos, const float* dir, int64_t n, const float basecube[4],
                               int maxlevel, const qbc_ray_hits* out, int on_device) {
   qbc::clear_error();
@@ -1360,6 +1485,7 @@ int launch_render_noalloc(qbc_ctx* c, const qbc::Batch& b, size_t smem, unsigned
   int per_sm = 0;
   QBC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, qbc::kThreads, smem));
   if (per_sm < 1) return fail(QBC_E_STATE, "render_kernel: no block fits on an SM with %zu B shared memory", smem);
+  if (c->blocks_per_sm > 0) per_sm = std::min(per_sm, c->blocks_per_sm);
   int64_t blocks = std::min<int64_t>((int64_t)per_sm * c->sm_count, ((int64_t)b.tiles_total + 3) / 4);
   blocks = std::max<int64_t>(blocks, 1);
   kern<<<(unsigned)blocks, qbc::kThreads, smem, c->stream>>>(device_scene(c), b, queue, qbc::Wave{});
@@ -1413,9 +1539,10 @@ extern "C" int qbc_render_views_noalloc(qbc_ctx* c, const qbc_view* views, const
       qbc::ViewJob& J = b.job[i];
       J.v = views[a + i];
       J.o = outs[a + i];
-      J.tiles_x = (views[a + i].width_px + 7) / 8;
+      const int tw = 1 << c->tile_shift, th = 32 >> c->tile_shift;
+      J.tiles_x = (views[a + i].width_px + tw - 1) / tw;
       J.tile_begin = tiles;
-      tiles += J.tiles_x * ((views[a + i].height_px + 3) / 4);
+      tiles += J.tiles_x * ((views[a + i].height_px + th - 1) / th);
       maxlevel = std::max(maxlevel, views[a + i].maxlevel);
       exact = exact && qbc::cube_shift_exact(views[a + i]);
     }
@@ -1423,6 +1550,7 @@ extern "C" int qbc_render_views_noalloc(qbc_ctx* c, const qbc_view* views, const
     b.tiles_total = tiles;
     b.max_level = maxlevel;
     b.service_min = c->service_min;
+    b.tile_shift = c->tile_shift;
     const size_t smem = ((size_t)(dyn ? 3 : 2) * maxlevel + qbc::kPixWords) * qbc::kThreads * sizeof(uint32_t);
     unsigned int* q = queues + l;
     if (exact)

@@ -21,7 +21,7 @@ constexpr int kPixWords = 28;  // per-lane pixel state words in shared memory
 struct ViewJob {
   qbc_view v;
   qbc_outputs o;  // device pointers
-  int32_t tiles_x;      // 8-pixel-wide warp tiles per row
+  int32_t tiles_x;      // warp tiles per row
   int32_t tile_begin;   // first global tile index of this view
   int64_t pixel_begin;  // first pixel index of this view within the batch
 };
@@ -32,6 +32,7 @@ struct Batch {
   int32_t tiles_total;
   int32_t max_level;    // largest maxlevel of the batch: stack depth
   int32_t service_min;  // lanes that must wait before a warp services them
+  int32_t tile_shift;   // warp tile: 2^tile_shift x 32 / 2^tile_shift pixels
 };
 
 // ---- main() helpers (octree_fsh.c:381-395 and GLSL built-ins) ----
@@ -433,7 +434,8 @@ struct Shader {
   }
 };
 
-// Global tile queue: tiles are 8x4 pixel warp tiles, numbered view by view.
+// Global tile queue: 32-pixel warp tiles (8x4 by default), numbered view by
+// view.
 __device__ __forceinline__ int tile_view(const Batch& b, int tile) {
   int lo = 0, hi = b.n - 1;
   while (lo < hi) {
@@ -535,8 +537,9 @@ __global__ void __launch_bounds__(kThreads) render_kernel(DevScene sc, const __g
             const int vi = tile_view(batch, chunk);
             const ViewJob& J = batch.job[vi];
             const int t = chunk - J.tile_begin;
-            const int x = (t % J.tiles_x) * 8 + (slot & 7);
-            const int y = (t / J.tiles_x) * 4 + (slot >> 3);
+            const int sh = batch.tile_shift;
+            const int x = ((t % J.tiles_x) << sh) + (slot & ((1 << sh) - 1));
+            const int y = (t / J.tiles_x) * (32 >> sh) + (slot >> sh);
             if (x < J.v.width_px && y < J.v.height_px) {
               S.begin_pixel(vi, x, y, rp, rd);
               go = true;

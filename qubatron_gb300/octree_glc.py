@@ -151,6 +151,18 @@ class OctreeGLC:
         stats = self.render_views_ex(views, [b.outputs() for b in bufs], False, **kw)
         return bufs, stats
 
+    def autotune(self, views: Sequence[View], outputs: Sequence[Outputs], reps: int = 5, two_pass: bool = False,
+                 proposals: int = 0, proposal_level: int = 0, seed: int = 0) -> dict:
+        """qbc_autotune: time candidate tuning options on these views (device
+        outputs) and leave the fastest set; returns the chosen settings."""
+        n = len(views)
+        varr = (View * n)(*views)
+        oarr = (Outputs * n)(*outputs)
+        opts = _lib.RenderOpts(int(two_pass), int(proposals), 0, int(proposal_level), int(seed))
+        res = _lib.TuneResult()
+        check(self._lib.qbc_autotune(self.handle, varr, oarr, n, C.byref(opts), int(reps), C.byref(res)))
+        return res.as_dict()
+
     def graph_capture(self, views: Sequence[View], outputs: Sequence[Outputs], two_pass: bool = False,
                       proposals: int = 0, proposal_level: int = 0, seed: int = 0) -> "FrameGraph":
         """qbc_graph_capture: the frame (device outputs) as a CUDA graph."""

@@ -119,3 +119,35 @@ def test_library_errors_without_gpu(lib):
         pytest.skip("a GPU is present")
     assert rc in (-1, -2)
     assert lib.qbc_last_error()
+
+
+STRUCTS = [("View", "qbc_view"), ("Outputs", "qbc_outputs"), ("RayHits", "qbc_ray_hits"),
+           ("RenderOpts", "qbc_render_opts"), ("RenderStats", "qbc_render_stats"), ("TuneResult", "qbc_tune_result"),
+           ("TrainOpts", "qbc_train_opts"), ("TrainStats", "qbc_train_stats"), ("SceneDesc", "qbc_scene_desc")]
+
+
+def test_ctypes_structs_match_header(tmp_path):
+    """Size and every field offset of each ctypes mirror equal the C
+    compiler's layout of the header's struct."""
+    import ctypes as C
+    import subprocess
+    import qubatron_gb300._lib as L
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "qbcuda.h"', "int main(void) {"]
+    for py, c in STRUCTS:
+        lines.append(f'  printf("{py} size %zu\\n", sizeof({c}));')
+        for f in getattr(L, py)._fields_:
+            lines.append(f'  printf("{py} {f[0]} %zu\\n", offsetof({c}, {f[0]}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for ln in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        py, key, val = ln.split()
+        got[py, key] = int(val)
+    for py, _ in STRUCTS:
+        cls = getattr(L, py)
+        assert got[py, "size"] == C.sizeof(cls), py
+        for f in cls._fields_:
+            assert got[py, f[0]] == getattr(cls, f[0]).offset, (py, f[0])
