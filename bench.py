@@ -293,6 +293,10 @@ def run_gpu(args):
     ctx.upload_octree(False, scene.nodes)
     if args.service_min:
         ctx.set_option(qb._lib.OPT_SERVICE_MIN, args.service_min)
+    if args.tile_width:
+        ctx.set_option(qb._lib.OPT_TILE_WIDTH, args.tile_width)
+    if args.blocks_per_sm:
+        ctx.set_option(qb._lib.OPT_BLOCKS_PER_SM, args.blocks_per_sm)
 
     def render_plain(v, o, dev):
         ctx.render_views(v, o, on_device=dev)
@@ -355,7 +359,7 @@ def run_gpu(args):
             chars.apply(poses[frame])
 
     tuning = None
-    if args.autotune and not args.service_min:
+    if args.autotune and not (args.service_min or args.tile_width or args.blocks_per_sm):
         # tuning options (service threshold, warp tile, blocks per SM) picked
         # by timing this frame; untimed
         update(0)
@@ -531,7 +535,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--service-min", type=int, default=0, help="override the kernel's service threshold")
+    ap.add_argument("--service-min", type=int, default=0, help="set the service threshold (no autotune)")
+    ap.add_argument("--tile-width", type=int, default=0, help="set the warp tile width 4/8/16/32 (no autotune)")
+    ap.add_argument("--blocks-per-sm", type=int, default=0, help="set render blocks per SM (no autotune)")
     ap.add_argument("--workload", default=None)
     ap.add_argument("--train-steps", type=int, default=4000, help="occluder-network training steps")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
