@@ -35,6 +35,7 @@ extern "C" {
 #define QBC_E_NOMEM -3    /* device or host allocation failed */
 #define QBC_E_STATE -4    /* call not valid in this state */
 #define QBC_E_TIMEOUT -5  /* a bounded wait inside a kernel gave up */
+#define QBC_E_IO -6       /* a file could not be opened or read */
 
 /* ---- GL enums the reference passes as `type` (GL/gl.h values) ---- */
 #define QBC_GL_INT 0x1404
@@ -289,6 +290,49 @@ typedef struct qbc_render_stats
 } qbc_render_stats;
 
 int qbc_render_views_ex(qbc_ctx* ctx, const qbc_view* views, const qbc_outputs* outs, int n, int outputs_on_device, const qbc_render_opts* opts, qbc_render_stats* stats);
+
+/*
+ * Static edits on the device. The reference edits its host octree with
+ * octree_remove_point (src/qubatron/octree.c:182-218) and re-uploads each
+ * edited node as a one-node range (modelutil.c:345-440). qbc_tree_remove_points
+ * edits the tree held on the device directly, as n octree_remove_point calls
+ * in input order would: per point, walk its octets (basesize, levels as the
+ * tree was built); at the leaf, zero the parent's link to it and report the
+ * leaf's model index (modind) and the parent node (octind). A point whose walk
+ * meets an empty link reports -1 for both (the reference leaves the caller's
+ * values as they were); of several points of one leaf, the first in input
+ * order removes it and the rest report -1. A point with x <= -size at some
+ * level (the reference would read outside the node there) or a non-finite
+ * coordinate reports -1 and changes nothing. pts, modind and octind are host
+ * or device arrays per on_device; modind / octind may be null. Captured frame
+ * graphs see the edit (no buffer moves).
+ */
+int qbc_tree_remove_points(qbc_ctx* ctx, int tree, const float* pts, int64_t n, float basesize, int levels, int on_device, int32_t* modind, int32_t* octind, int64_t* removed);
+
+/*
+ * qmc flat model files, the reference's on-disk scene format (read by
+ * model_load_flat, src/qubatron/model.c:53-111; written by qmc,
+ * src/qubatron/qmc.c:275-327): .pnt, .nrm and .col hold one float3 per
+ * point, .rng holds int triples (first point index of a column, x index,
+ * y index).
+ *
+ * qbc_flat_read (host only, no GPU): the point count is the .pnt size in
+ * whole float3 (trailing bytes ignored); colours and normals are read for
+ * that many points (a shorter file leaves the rest 0); the range count is the
+ * .rng size in whole ints. Null arrays return only the counts; arrays are
+ * filled when their capacity (points, ints) suffices, else QBC_E_ARG.
+ * rng_path may be null (no ranges). A file that cannot be opened or read
+ * gives QBC_E_IO (the reference crashes on a missing .pnt).
+ *
+ * qbc_load_flat: qbc_flat_read, then what the reference's static model load
+ * does with it (modelutil.c:180-255): octree_insert_point of every point in
+ * file order into an empty tree (levels, basecube (0, S, S, S)), here built
+ * on the GPU, and the colours and normals uploaded as that tree's model.
+ * tree: 0 static, 1 dynamic. Counts out (any may be null); ranges as in
+ * qbc_flat_read.
+ */
+int qbc_flat_read(const char* pnt_path, const char* col_path, const char* nrm_path, const char* rng_path, float* pnts, float* cols, float* nrms, int64_t point_cap, int64_t* points, int32_t* ranges, int64_t range_cap, int64_t* range_ints);
+int qbc_load_flat(qbc_ctx* ctx, int tree, const char* pnt_path, const char* col_path, const char* nrm_path, const char* rng_path, float basesize, int levels, int64_t* points, int64_t* nodes, int32_t* ranges, int64_t range_cap, int64_t* range_ints);
 
 /*
  * Autotuner (not part of the reference). Times frames of these views

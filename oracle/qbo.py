@@ -140,6 +140,9 @@ def ref() -> C.CDLL | None:
         lib.qbref_remove.restype = None
         lib.qbref_trace.argtypes = [i32p, C.c_long, C.c_float, C.c_int, f32p, f32p, C.c_long, i32p, f32p]
         lib.qbref_trace.restype = None
+        lib.qbref_load_flat.argtypes = [C.c_char_p] * 4 + [f32p, f32p, f32p, C.c_long, i32p, C.c_long,
+                                                           C.POINTER(C.c_long)]
+        lib.qbref_load_flat.restype = C.c_long
         _ref = lib
     return _ref
 
@@ -283,3 +286,17 @@ def ref_trace(nodes: np.ndarray, basesize: float, levels: int, pos: np.ndarray, 
     lib.qbref_trace(nodes.ctypes.data_as(i32p), nodes.size // 12, basesize, levels, pos.ctypes.data_as(f32p),
                     dirs.ctypes.data_as(f32p), n, model.ctypes.data_as(i32p), tlf.ctypes.data_as(f32p))
     return model, tlf
+
+
+def ref_load_flat(prefix: str) -> dict:
+    """The reference's model_load_flat on prefix.{pnt,col,nrm,rng}: point
+    count, float3 arrays and range ints."""
+    lib = ref()
+    paths = [(prefix + e).encode() for e in (".pnt", ".col", ".nrm", ".rng")]
+    rc = C.c_long()
+    n = lib.qbref_load_flat(*paths, None, None, None, 0, None, 0, C.byref(rc))
+    vtx, col, nrm = (np.zeros((n, 3), np.float32) for _ in range(3))
+    rng = np.zeros(max(rc.value, 1), np.int32)
+    lib.qbref_load_flat(*paths, vtx.ctypes.data_as(f32p), col.ctypes.data_as(f32p), nrm.ctypes.data_as(f32p), n,
+                        rng.ctypes.data_as(i32p), rng.size, C.byref(rc))
+    return {"points": vtx, "colors": col, "normals": nrm, "ranges": rng[:rc.value]}

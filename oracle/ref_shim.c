@@ -1,10 +1,13 @@
 /*
- * Flat entry points over the reference's own src/qubatron/octree.c, compiled
- * from the reference sources by oracle/build_ref.sh into oracle/_ref. Test
- * infrastructure only: it pins the oracle's restatement (qbo_octree.c,
- * qbo_trace.c) to the reference's CPU insertion and static-tree traversal.
+ * Flat entry points over the reference's own src/qubatron/octree.c and
+ * src/qubatron/model.c, compiled from the reference sources by
+ * oracle/build_ref.sh into oracle/_ref. Test infrastructure only: it pins the
+ * oracle's restatement (qbo_octree.c, qbo_trace.c) to the reference's CPU
+ * insertion and static-tree traversal, and the library's flat-file reader to
+ * the reference's model_load_flat.
  */
 #include "octree.c" /* declarations only: included below level 0 */
+#include "model.c"
 
 #include <string.h>
 
@@ -74,4 +77,24 @@ void qbref_trace(const int* nodes, long n_nodes, float basesize, int levels, con
         out_tlf[i * 4 + 2] = tlf.z;
         out_tlf[i * 4 + 3] = tlf.w;
     }
+}
+
+/* model_load_flat (model.c:53-111) on the four paths; returns the point count
+ * and copies the float3 arrays (3 floats per point) and the range ints when
+ * they fit. */
+long qbref_load_flat(const char* pnt, const char* col, const char* nrm, const char* rng, float* vtx, float* cols,
+                     float* nrms, long cap, int* ranges, long rcap, long* range_count)
+{
+    model_t m = model_init();
+    model_load_flat(&m, (char*) pnt, (char*) col, (char*) nrm, (char*) rng);
+    long n = m.point_count;
+    if (vtx != NULL && n <= cap)
+    {
+        memcpy(vtx, m.vertexes, (size_t) n * 3 * sizeof(float));
+        memcpy(cols, m.colors, (size_t) n * 3 * sizeof(float));
+        memcpy(nrms, m.normals, (size_t) n * 3 * sizeof(float));
+    }
+    *range_count = m.range_count;
+    if (ranges != NULL && m.range_count <= rcap) memcpy(ranges, m.ranges, (size_t) m.range_count * sizeof(int));
+    return n;
 }

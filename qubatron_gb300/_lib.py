@@ -34,7 +34,7 @@ PX_OOB = 1 << 7
 SCENE_FLOOR = 0
 SCENE_ROOM = 1
 
-ERRORS = {-1: "QBC_E_ARG", -2: "QBC_E_CUDA", -3: "QBC_E_NOMEM", -4: "QBC_E_STATE", -5: "QBC_E_TIMEOUT"}
+ERRORS = {-1: "QBC_E_ARG", -2: "QBC_E_CUDA", -3: "QBC_E_NOMEM", -4: "QBC_E_STATE", -5: "QBC_E_TIMEOUT", -6: "QBC_E_IO"}
 
 
 class QbcError(RuntimeError):
@@ -199,6 +199,12 @@ SIGNATURES = {
     "qbc_render_views_ex": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int, C.c_int,
                                       C.POINTER(RenderOpts), C.POINTER(RenderStats)]),
     "qbc_render_views_noalloc": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int]),
+    "qbc_tree_remove_points": (C.c_int, [C.c_void_p, C.c_int, c_float_p, C.c_int64, C.c_float, C.c_int, C.c_int,
+                                         C.POINTER(C.c_int32), C.POINTER(C.c_int32), c_int64_p]),
+    "qbc_flat_read": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, c_float_p, c_float_p, c_float_p,
+                                C.c_int64, c_int64_p, C.POINTER(C.c_int32), C.c_int64, c_int64_p]),
+    "qbc_load_flat": (C.c_int, [C.c_void_p, C.c_int, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_float,
+                                C.c_int, c_int64_p, c_int64_p, C.POINTER(C.c_int32), C.c_int64, c_int64_p]),
     "qbc_autotune": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int, C.POINTER(RenderOpts), C.c_int,
                                C.POINTER(TuneResult)]),
     "qbc_graph_capture": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int, C.POINTER(RenderOpts),

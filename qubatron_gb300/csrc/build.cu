@@ -132,6 +132,70 @@ __global__ void link_kernel(const uint64_t* __restrict__ prefix, const uint32_t*
   }
 }
 
+// ---- octree_remove_point (octree.c:182-218) for a batch of points ----
+//
+// Per point, the walk of octree_remove_point on the unedited tree: size
+// halves from the basecube edge for levels + 1 steps; (int)(c / size) % 2 with
+// C truncation and remainder; at level == levels the current node is the
+// leaf, reported with its parent and the parent's octet. Points of different
+// leaves do not meet (a removal only cuts a parent's link to its leaf), so
+// the batch equals sequential calls once duplicates of a leaf are resolved:
+// the first in input order removes it, the later ones find the link cut.
+// key = leaf << 32 | point index, or ~0 when the point removes nothing.
+__global__ void remove_walk_kernel(const int32_t* __restrict__ child, const int32_t* __restrict__ model,
+                                   int64_t n_nodes, const float* __restrict__ pts, int64_t n, float basesize,
+                                   int levels, uint64_t* __restrict__ keys, int32_t* __restrict__ parent,
+                                   int8_t* __restrict__ poct) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float x = pts[3 * i], y = pts[3 * i + 1], z = pts[3 * i + 2];
+    uint64_t key = ~0ull;
+    float size = basesize;
+    int32_t index = 0, lindex = 0;
+    int loctet = 0;
+    for (int level = 0; level < levels + 1; ++level) {
+      size /= 2.0f;
+      const float qx = x / size, qy = y / size, qz = z / size;
+      // a float -> int conversion outside int range is undefined in C: skip
+      if (!(fabsf(qx) < 2147483648.0f && fabsf(qy) < 2147483648.0f && fabsf(qz) < 2147483648.0f)) break;
+      int octet = (int)qx % 2;
+      const int yi = (int)qy % 2, zi = (int)qz % 2;
+      if (yi == 0) octet += 2;
+      if (zi == 0) octet += 4;
+      if (level == levels) {
+        key = ((uint64_t)(uint32_t)index << 32) | (uint64_t)i;
+        parent[i] = lindex;
+        poct[i] = (int8_t)loctet;
+        break;
+      }
+      if (octet < 0) break;  // x <= -size: the reference would read oct[-1]
+      lindex = index;
+      loctet = octet;
+      index = child[(int64_t)index * 8 + octet];
+      if (index <= 0 || index >= n_nodes) break;  // empty link (or not a node of this tree)
+    }
+    keys[i] = key;
+  }
+}
+
+// Sorted keys: the first point of each leaf cuts the parent's link and
+// reports the leaf's model index and the parent node.
+__global__ void remove_apply_kernel(const uint64_t* __restrict__ keys, int64_t n, int32_t* __restrict__ child,
+                                    const int32_t* __restrict__ model, const int32_t* __restrict__ parent,
+                                    const int8_t* __restrict__ poct, int32_t* __restrict__ modind,
+                                    int32_t* __restrict__ octind, unsigned long long* __restrict__ removed) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+    const uint64_t k = keys[j];
+    if (k == ~0ull) continue;
+    const uint32_t leaf = (uint32_t)(k >> 32);
+    if (j > 0 && (uint32_t)(keys[j - 1] >> 32) == leaf) continue;
+    const int64_t i = (int64_t)(k & 0xFFFFFFFFull);
+    child[(int64_t)parent[i] * 8 + poct[i]] = 0;
+    modind[i] = model[leaf];
+    octind[i] = parent[i];
+    atomicAdd(removed, 1ull);
+  }
+}
+
 int grid_for(int64_t n) {
   int64_t b = (n + 255) / 256;
   return (int)std::max<int64_t>(1, std::min<int64_t>(b, 65535));
@@ -230,6 +294,45 @@ int build_nodes(const float* d_pts, const int32_t* d_octets, int64_t n, float ba
     return fail(QBC_E_NOMEM, "tree build: %s", ex.what());
   }
   tgt->n_nodes = total;
+  return QBC_OK;
+}
+
+int remove_points(int32_t* child, const int32_t* model, int64_t n_nodes, const float* d_pts, int64_t n,
+                  float basesize, int levels, int32_t* d_modind, int32_t* d_octind, int64_t* removed,
+                  cudaStream_t stream, int64_t* launches) {
+  if (n <= 0) {
+    if (removed) *removed = 0;
+    return QBC_OK;
+  }
+  if (n >= (int64_t)0xFFFFFFFF) return fail(QBC_E_ARG, "tree remove: %lld points in one call", (long long)n);
+  try {
+    auto pol = thrust::cuda::par.on(stream);
+    thrust::device_vector<uint64_t> keys(n);
+    thrust::device_vector<int32_t> parent(n);
+    thrust::device_vector<int8_t> poct(n);
+    thrust::device_vector<unsigned long long> count(1, 0ull);
+    cudaMemsetAsync(d_modind, 0xFF, (size_t)n * 4, stream);  // -1: nothing removed
+    cudaMemsetAsync(d_octind, 0xFF, (size_t)n * 4, stream);
+    remove_walk_kernel<<<grid_for(n), 256, 0, stream>>>(child, model, n_nodes, d_pts, n, basesize, levels,
+                                                        thrust::raw_pointer_cast(keys.data()),
+                                                        thrust::raw_pointer_cast(parent.data()),
+                                                        thrust::raw_pointer_cast(poct.data()));
+    thrust::sort(pol, keys.begin(), keys.end());
+    remove_apply_kernel<<<grid_for(n), 256, 0, stream>>>(thrust::raw_pointer_cast(keys.data()), n, child, model,
+                                                         thrust::raw_pointer_cast(parent.data()),
+                                                         thrust::raw_pointer_cast(poct.data()), d_modind, d_octind,
+                                                         thrust::raw_pointer_cast(count.data()));
+    *launches += 3;  // walk, sort, apply
+    unsigned long long h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, thrust::raw_pointer_cast(count.data()), sizeof(h), cudaMemcpyDeviceToHost,
+                                    stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(QBC_E_CUDA, "tree remove: %s", cudaGetErrorString(e));
+    if (removed) *removed = (int64_t)h;
+  } catch (const std::exception& ex) {
+    return fail(QBC_E_NOMEM, "tree remove: %s", ex.what());
+  }
   return QBC_OK;
 }
 

@@ -604,3 +604,71 @@ extern "C" int qbc_scene_generate(const qbc_scene_desc* d, float* pnts, float* n
   }
   return QBC_OK;
 }
+
+// ---------------------------------------------------------------------------
+// qmc flat model files (model_load_flat, src/qubatron/model.c:53-111; the
+// writer is qmc.c:275-327): .pnt / .nrm / .col float3 per point, .rng int
+// triples (first point index of a column, x index, y index)
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct File {
+  FILE* f = nullptr;
+  ~File() {
+    if (f) std::fclose(f);
+  }
+};
+
+int open_sized(const char* path, File& file, int64_t* bytes) {
+  file.f = std::fopen(path, "rb");
+  if (!file.f) return fail(QBC_E_IO, "qmc flat file: cannot open %s", path);
+  if (std::fseek(file.f, 0, SEEK_END) != 0) return fail(QBC_E_IO, "qmc flat file: cannot seek %s", path);
+  const long end = std::ftell(file.f);
+  if (end < 0 || std::fseek(file.f, 0, SEEK_SET) != 0) return fail(QBC_E_IO, "qmc flat file: cannot size %s", path);
+  *bytes = end;
+  return QBC_OK;
+}
+
+// Read up to `want` bytes into dst; the rest of `want` stays zero (a file
+// shorter than the point file).
+int read_into(File& file, const char* path, void* dst, int64_t want, int64_t have) {
+  const int64_t n = std::min(want, have);
+  if (n > 0 && std::fread(dst, 1, (size_t)n, file.f) != (size_t)n)
+    return fail(QBC_E_IO, "qmc flat file: short read of %s", path);
+  if (want > n) std::memset(static_cast<char*>(dst) + n, 0, (size_t)(want - n));
+  return QBC_OK;
+}
+
+}  // namespace
+
+extern "C" int qbc_flat_read(const char* pnt_path, const char* col_path, const char* nrm_path, const char* rng_path,
+                             float* pnts, float* cols, float* nrms, int64_t point_cap, int64_t* points,
+                             int32_t* ranges, int64_t range_cap, int64_t* range_ints) {
+  qbc::clear_error();
+  if (!pnt_path || !col_path || !nrm_path || !points) return fail(QBC_E_ARG, "qbc_flat_read: null path or count");
+  File fp, fc, fn, fr;
+  int64_t bp = 0, bc = 0, bn = 0, br = 0;
+  int rc = open_sized(pnt_path, fp, &bp);
+  if (!rc) rc = open_sized(col_path, fc, &bc);
+  if (!rc) rc = open_sized(nrm_path, fn, &bn);
+  if (!rc && rng_path) rc = open_sized(rng_path, fr, &br);
+  if (rc) return rc;
+  // the point count is the .pnt size in whole float3 (model.c:59-63)
+  const int64_t n = bp / 12;
+  const int64_t nr = rng_path ? br / 4 : 0;
+  *points = n;
+  if (range_ints) *range_ints = nr;
+  if (pnts || cols || nrms) {
+    if (!pnts || !cols || !nrms) return fail(QBC_E_ARG, "qbc_flat_read: give all three point arrays or none");
+    if (point_cap < n) return fail(QBC_E_ARG, "qbc_flat_read: %lld points, capacity %lld", (long long)n, (long long)point_cap);
+    if ((rc = read_into(fp, pnt_path, pnts, n * 12, bp))) return rc;
+    if ((rc = read_into(fc, col_path, cols, n * 12, bc))) return rc;
+    if ((rc = read_into(fn, nrm_path, nrms, n * 12, bn))) return rc;
+  }
+  if (ranges && rng_path) {
+    if (range_cap < nr) return fail(QBC_E_ARG, "qbc_flat_read: %lld range ints, capacity %lld", (long long)nr, (long long)range_cap);
+    if ((rc = read_into(fr, rng_path, ranges, nr * 4, br))) return rc;
+  }
+  return QBC_OK;
+}

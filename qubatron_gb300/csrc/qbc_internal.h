@@ -34,4 +34,12 @@ struct BuildTarget {
 int build_nodes(const float* d_pts, const int32_t* d_octets, int64_t n, float basesize, int levels,
                 int64_t first_index, cudaStream_t stream, BuildTarget* tgt);
 
+// octree_remove_point (octree.c:182-218) of n points in order, on a device
+// tree (child: 8 int32 per node, model: 1 per node): cuts the links in place,
+// reports modind / octind per point (-1 where nothing was removed) into
+// device arrays and the number removed.
+int remove_points(int32_t* child, const int32_t* model, int64_t n_nodes, const float* d_pts, int64_t n,
+                  float basesize, int levels, int32_t* d_modind, int32_t* d_octind, int64_t* removed,
+                  cudaStream_t stream, int64_t* launches);
+
 }  // namespace qbc

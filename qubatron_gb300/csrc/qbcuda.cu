@@ -11,6 +11,7 @@
 #include <cstring>
 #include <mutex>
 #include <memory>
+#include <new>
 #include <vector>
 
 #include "qbc_internal.h"
@@ -553,6 +554,97 @@ extern "C" int qbc_build_tree_paths(qbc_ctx* c, int tree, const int32_t* octets,
   if (n > 0 && !octets) return fail(QBC_E_ARG, "qbc_build_tree_paths: null octets");
   if (n == 0) octets = reinterpret_cast<const int32_t*>(&n);
   return build_into(c, tree, nullptr, octets, n, 1.0f, levels, first_index, on_device);
+}
+
+extern "C" int qbc_load_flat(qbc_ctx* c, int tree, const char* pnt_path, const char* col_path, const char* nrm_path,
+                             const char* rng_path, float basesize, int levels, int64_t* points, int64_t* nodes,
+                             int32_t* ranges, int64_t range_cap, int64_t* range_ints) {
+  qbc::clear_error();
+  if (!c || tree < 0 || tree > 1) return fail(QBC_E_ARG, "qbc_load_flat: bad context or tree id");
+  int64_t n = 0, nr = 0;
+  int rc = qbc_flat_read(pnt_path, col_path, nrm_path, rng_path, nullptr, nullptr, nullptr, 0, &n, nullptr, 0, &nr);
+  if (rc) return rc;
+  std::vector<float> p, col, nrm;
+  try {
+    p.resize((size_t)n * 3);
+    col.resize((size_t)n * 3);
+    nrm.resize((size_t)n * 3);
+  } catch (const std::bad_alloc&) {
+    return fail(QBC_E_NOMEM, "qbc_load_flat: host arrays for %lld points", (long long)n);
+  }
+  rc = qbc_flat_read(pnt_path, col_path, nrm_path, rng_path, p.data(), col.data(), nrm.data(), n, &n, ranges,
+                     range_cap, &nr);
+  if (rc) return rc;
+  // the reference's load: insert every point in file order, upload the
+  // colours and normals as the tree's model (modelutil.c:180-255)
+  const size_t bytes = (size_t)n * 12;
+  if (n > 0) {
+    rc = upload_impl(c, col.data(), QBC_GL_FLOAT, bytes, 12, 0, bytes, tree ? QBC_DYNAMIC_COLOR : QBC_STATIC_COLOR,
+                     false);
+    if (!rc)
+      rc = upload_impl(c, nrm.data(), QBC_GL_FLOAT, bytes, 12, 0, bytes,
+                       tree ? QBC_DYNAMIC_NORMAL : QBC_STATIC_NORMAL, false);
+    if (rc) return rc;
+  }
+  const float* src = n > 0 ? p.data() : reinterpret_cast<const float*>(&n);
+  rc = build_into(c, tree, src, nullptr, n, basesize, levels, 0, 0);
+  if (rc) return rc;
+  if (points) *points = n;
+  if (nodes) *nodes = c->tree[tree].n;
+  if (range_ints) *range_ints = nr;
+  return QBC_OK;
+}
+
+extern "C" int qbc_tree_remove_points(qbc_ctx* c, int tree, const float* pts, int64_t n, float basesize, int levels,
+                                      int on_device, int32_t* modind, int32_t* octind, int64_t* removed) {
+  qbc::clear_error();
+  if (!c || tree < 0 || tree > 1 || n < 0 || (n > 0 && !pts)) return fail(QBC_E_ARG, "qbc_tree_remove_points: bad argument");
+  if (!(basesize > 0.0f) || levels < 0 || levels > QBC_MAX_LEVEL)
+    return fail(QBC_E_ARG, "qbc_tree_remove_points: basesize > 0 and levels 0..%d required", QBC_MAX_LEVEL);
+  if (c->tree[tree].n == 0) return fail(QBC_E_STATE, "qbc_tree_remove_points: no tree uploaded or built");
+  QBC_CUDA(cudaSetDevice(c->device));
+  if (n == 0) {
+    if (removed) *removed = 0;
+    return QBC_OK;
+  }
+  // device arrays: the caller's when on_device, else staged
+  void* tmp = nullptr;
+  const size_t pbytes = (size_t)n * 12, obytes = (size_t)n * 4;
+  const float* dp = pts;
+  int32_t* dm = modind;
+  int32_t* dq = octind;
+  const bool stage_out = !on_device || !modind || !octind;
+  size_t need = (on_device ? 0 : pbytes) + (stage_out ? 2 * obytes : 0);
+  if (need) {
+    cudaError_t e = cudaMalloc(&tmp, need);
+    if (e != cudaSuccess) return fail(QBC_E_NOMEM, "qbc_tree_remove_points: %s", cudaGetErrorString(e));
+  }
+  char* t = static_cast<char*>(tmp);
+  int rc = QBC_OK;
+  if (!on_device) {
+    cudaError_t e = cudaMemcpyAsync(t, pts, pbytes, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "qbc_tree_remove_points: copy points");
+    dp = reinterpret_cast<const float*>(t);
+    t += pbytes;
+  }
+  if (stage_out) {
+    dm = reinterpret_cast<int32_t*>(t);
+    dq = reinterpret_cast<int32_t*>(t + obytes);
+  }
+  if (!rc)
+    rc = qbc::remove_points(reinterpret_cast<int32_t*>(c->tree[tree].child), c->tree[tree].model, c->tree[tree].n,
+                            dp, n, basesize, levels, dm, dq, removed, c->stream, &c->launches);
+  if (!rc && stage_out) {
+    // results to the caller's arrays (host, or device when only one was given)
+    const cudaMemcpyKind k = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    cudaError_t e = cudaSuccess;
+    if (modind) e = cudaMemcpyAsync(modind, dm, obytes, k, c->stream);
+    if (e == cudaSuccess && octind) e = cudaMemcpyAsync(octind, dq, obytes, k, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "qbc_tree_remove_points: copy results");
+  }
+  if (tmp) cudaFree(tmp);
+  return rc;
 }
 
 extern "C" int qbc_download_tree(qbc_ctx* c, int tree, int32_t* nodes, int64_t cap, int64_t* n_nodes) {

@@ -52,9 +52,10 @@ class Octree:
                                                 int(first_index)))
 
     def remove_point(self, point) -> tuple:
-        """octree_remove_point (octree.c:182-218) -> (model index, parent node)."""
+        """octree_remove_point (octree.c:182-218) -> (model index, parent node),
+        (-1, -1) when the point's walk meets an empty link."""
         p = (C.c_float * 3)(*[float(x) for x in point])
-        m, o = C.c_int32(), C.c_int32()
+        m, o = C.c_int32(-1), C.c_int32(-1)
         check(self._lib.qbc_octree_remove_point(self.handle, p, C.byref(m), C.byref(o)))
         return m.value, o.value
 

@@ -151,6 +151,33 @@ class OctreeGLC:
         stats = self.render_views_ex(views, [b.outputs() for b in bufs], False, **kw)
         return bufs, stats
 
+    def remove_points(self, dynamic: bool, points, basesize: float = 1800.0, levels: int = 12):
+        """qbc_tree_remove_points on host points: octree_remove_point of each
+        point in order, on the device tree. Returns (modind, octind, removed)."""
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+        n = pts.shape[0]
+        mod = np.zeros(n, np.int32)
+        oct_ = np.zeros(n, np.int32)
+        rem = C.c_int64()
+        i32 = C.POINTER(C.c_int32)
+        check(self._lib.qbc_tree_remove_points(self.handle, 1 if dynamic else 0, pts.ctypes.data_as(_lib.c_float_p), n,
+                                               basesize, levels, 0, mod.ctypes.data_as(i32), oct_.ctypes.data_as(i32),
+                                               C.byref(rem)))
+        return mod, oct_, rem.value
+
+    def load_flat(self, prefix: str, dynamic: bool = False, basesize: float = 1800.0, levels: int = 12) -> dict:
+        """qbc_load_flat: read prefix.{pnt,col,nrm,rng}, build the tree on the
+        GPU in file order, upload the model; returns counts and ranges."""
+        from .flatfile import paths
+        p = [s.encode() for s in paths(prefix)]
+        n, nodes, nr = C.c_int64(), C.c_int64(), C.c_int64()
+        check(self._lib.qbc_flat_read(p[0], p[1], p[2], p[3], None, None, None, 0, C.byref(n), None, 0, C.byref(nr)))
+        rng = np.zeros(max(nr.value, 1), np.int32)
+        check(self._lib.qbc_load_flat(self.handle, 1 if dynamic else 0, p[0], p[1], p[2], p[3], basesize, levels,
+                                      C.byref(n), C.byref(nodes), rng.ctypes.data_as(C.POINTER(C.c_int32)), rng.size,
+                                      C.byref(nr)))
+        return {"points": n.value, "nodes": nodes.value, "ranges": rng[:nr.value]}
+
     def autotune(self, views: Sequence[View], outputs: Sequence[Outputs], reps: int = 5, two_pass: bool = False,
                  proposals: int = 0, proposal_level: int = 0, seed: int = 0) -> dict:
         """qbc_autotune: time candidate tuning options on these views (device

@@ -4,7 +4,8 @@ Run in a checkout that has the reference sources (default /root/reference):
 
     python tests/golden/make_golden.py [REFERENCE_ROOT]
 
-It compiles the reference's src/qubatron/octree.c (oracle/build_ref.sh) and
+It compiles the reference's src/qubatron/octree.c and model.c
+(oracle/build_ref.sh) and
 records what that code produces:
 
 * ``five_point.npz``   the 5-point OCTTEST scene of modelutil.c:91-129:
@@ -14,7 +15,16 @@ records what that code produces:
                        SHA-256 of the node array from octree_insert_point, node
                        array from octree_insert_path over the same octets,
                        octree_remove_point results, and octree_trace_line
-                       results for random and edge-case rays.
+                       results for random and edge-case rays;
+* ``remove_edges.npz`` octree_remove_point called in order on the 5-point
+                       tree for duplicates, misses and points just below 0
+                       (walks the reference defines), with the node array
+                       after each call sequence;
+* ``flat/small.{pnt,col,nrm,rng}`` + ``flat_small.npz``  a 2,000-point qmc
+                       flat model (7 trailing bytes after the last point, a
+                       partial int after the last range) and what the
+                       reference's model_load_flat (src/qubatron/model.c)
+                       reads from it.
 
 octree_trace_line covers the static single-tree traversal; rays on which
 more than 4 basecube faces pass the entry test overflow the reference's
@@ -145,6 +155,37 @@ def main(root: str) -> None:
                         removed_sha256=np.frombuffer(hashlib.sha256(rm.tobytes()).digest(), np.uint8),
                         ray_pos=pos, ray_dir=dirs, ref_model=model, ref_tlf=tlf)
     print("floor50k:", nodes.shape[0], "nodes,", len(pos), "rays,", int((tlf[:, 3] >= 0).sum()), "leaf hits")
+
+    # ---- octree_remove_point edge cases on the 5-point tree ----
+    rm_pts = np.array([[10, 690, 10], [10, 690, 10], [10.1, 690.1, 10.1], [10, 340, 690], [900, 900, 900],
+                       [-0.1, 340, 10], [-0.2, 10, 10], [690, 10, 690], [10, 10, 10], [690.2, 10.2, 690.2],
+                       [1799.9, 0.1, 0.1], [10, 340, 10]], np.float32)
+    rm5 = nodes5.copy()
+    rm5_out = np.full((len(rm_pts), 2), -1, np.int32)
+    for k, p in enumerate(rm_pts):
+        m = np.full(1, -1, np.int32)
+        o = np.full(1, -1, np.int32)
+        lib.qbref_remove(rm5.ctypes.data_as(qbo.i32p), rm5.shape[0], S, LEVELS, p.ctypes.data_as(qbo.f32p),
+                         m.ctypes.data_as(qbo.i32p), o.ctypes.data_as(qbo.i32p))
+        rm5_out[k] = (m[0], o[0])
+    np.savez_compressed(os.path.join(HERE, "remove_edges.npz"), nodes=nodes5, points=rm_pts, out=rm5_out,
+                        nodes_after=rm5)
+    print("remove_edges:", int((rm5_out[:, 1] >= 0).sum()), "of", len(rm_pts), "removed")
+
+    # ---- qmc flat model files, read by the reference's model_load_flat ----
+    from qubatron_gb300.flatfile import write_flat
+    fpts, fnrm, fcol = floor_points(2000)
+    rng_ints = np.random.default_rng(15).integers(0, 2000, 3 * 40).astype(np.int32)
+    os.makedirs(os.path.join(HERE, "flat"), exist_ok=True)
+    prefix = os.path.join(HERE, "flat", "small")
+    write_flat(prefix, fpts, fnrm, fcol, rng_ints)
+    with open(prefix + ".pnt", "ab") as f:
+        f.write(bytes(range(7)))  # not a whole float3: ignored by the reader
+    with open(prefix + ".rng", "ab") as f:
+        f.write(bytes([1, 2]))  # not a whole int: ignored
+    got = qbo.ref_load_flat(prefix)
+    np.savez_compressed(os.path.join(HERE, "flat_small.npz"), **got)
+    print("flat_small:", got["points"].shape[0], "points,", got["ranges"].size, "range ints")
 
 
 if __name__ == "__main__":

@@ -85,3 +85,78 @@ def test_render_after_gpu_build(ctx, oracle, floor50k_scene):
     v = view_setup(320, 240, (903.7, 421.3, 1702.9), (0.0, -0.3, 0.0), 0.0, 10, LEVELS, S, 0, 0.0)
     r = oracle.render(oracle_scene(oracle, s.nodes, s.colors, s.normals), oracle.QboView.from_bytes(v.to_bytes()))
     compare_frame(gpu_frame(ctx, v), r, "render after GPU build")
+
+
+def test_load_flat_builds_and_uploads(ctx, tmp_path):
+    """qbc_load_flat: the reference's static load (model_load_flat, then
+    octree_insert_point per point in file order, then the uploads) with the
+    build on the GPU: the node array equals the producer's (pinned to the
+    reference), and the frame equals one of the same scene uploaded."""
+    from qubatron_gb300 import Octree, scenes, view_setup
+    from qubatron_gb300.flatfile import write_flat
+    from helpers import upload_scene
+    pts, nrm, col = scenes.generate_points(scenes.scaled_spec("floor1m", 60_000))
+    ranges = np.arange(30, dtype=np.int32)
+    prefix = str(tmp_path / "scene")
+    write_flat(prefix, pts, nrm, col, ranges)
+    got = ctx.load_flat(prefix)
+    t = Octree(S, LEVELS)
+    t.insert_points(pts)
+    assert got["points"] == len(pts) and got["nodes"] == t.nodes.shape[0]
+    assert np.array_equal(got["ranges"], ranges)
+    np.testing.assert_array_equal(ctx.download_tree(False), t.nodes)
+    v = view_setup(320, 240, (903.7, 421.3, 1702.9), (0.0, -0.3, 0.0), 0.0, 10, LEVELS, S, 0, 0.0)
+    loaded = ctx.render_host([v], ("rgba8", "leaf", "isp"))[0]
+    import qubatron_gb300 as qb
+    with qb.OctreeGLC(0) as other:
+        upload_scene(other, t.nodes, col, nrm)
+        direct = other.render_host([v], ("rgba8", "leaf", "isp"))[0]
+    for k in ("rgba8", "leaf", "isp"):
+        assert np.array_equal(loaded[k], direct[k]), k
+
+
+def test_remove_points_matches_reference(ctx, floor50k, floor50k_scene):
+    """One batch of qbc_tree_remove_points equals the reference's
+    octree_remove_point called in order (fixtures recorded from its own
+    octree.c): reported model / parent indices and the edited node array."""
+    s = floor50k_scene
+    ctx.build_tree(False, s.points, S, LEVELS)
+    idx = floor50k["remove_idx"]
+    mod, oct_, removed = ctx.remove_points(False, s.points[idx])
+    np.testing.assert_array_equal(np.stack([mod, oct_], 1), floor50k["remove_out"])
+    assert removed == int((floor50k["remove_out"][:, 1] >= 0).sum())
+    assert sha(ctx.download_tree(False)) == floor50k["removed_sha256"].tobytes()
+
+
+def test_remove_points_edge_cases_match_reference(ctx):
+    import os
+    from conftest import ROOT
+    d = np.load(os.path.join(ROOT, "tests", "golden", "remove_edges.npz"))
+    from helpers import upload_scene
+    n = d["nodes"]
+    upload_scene(ctx, n, np.ones((5, 3), np.float32), np.ones((5, 3), np.float32))
+    mod, oct_, removed = ctx.remove_points(False, d["points"])
+    np.testing.assert_array_equal(np.stack([mod, oct_], 1), d["out"])
+    np.testing.assert_array_equal(ctx.download_tree(False), d["nodes_after"])
+
+
+def test_remove_points_batches_equal_sequential_calls(ctx):
+    """Duplicates, misses and repeated batches against the producer's
+    sequential octree_remove_point (itself pinned to the reference)."""
+    from qubatron_gb300 import Octree, scenes
+    pts, _, _ = scenes.generate_points(scenes.scaled_spec("room20m", 30000))
+    t = Octree(S, LEVELS)
+    t.insert_points(pts)
+    ctx.build_tree(False, pts, S, LEVELS)
+    rng = np.random.default_rng(5)
+    for batch in range(3):
+        pick = pts[rng.choice(len(pts), 700)]  # with repeats
+        miss = rng.uniform(0, S, (50, 3)).astype(np.float32)
+        b = np.concatenate([pick, miss, pick[:40]])[rng.permutation(790)]
+        want = np.full((len(b), 2), -1, np.int32)
+        for k, p in enumerate(b):
+            want[k] = t.remove_point(p)
+        mod, oct_, removed = ctx.remove_points(False, b)
+        np.testing.assert_array_equal(np.stack([mod, oct_], 1), want)
+        assert removed == int((want[:, 1] >= 0).sum()) > 0
+        np.testing.assert_array_equal(ctx.download_tree(False), t.nodes)
