@@ -118,13 +118,16 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def prepare(workload_name: str):
+def prepare(workload_name: str, host_nodes: bool = True):
+    """Scene, views and character of a workload. House-scale scenes skip the
+    host node array unless host_nodes; the GPU builds their tree."""
     from qubatron_gb300 import scenes
     w = scenes.WORKLOADS[workload_name]
     t = time.time()
-    scene = scenes.make_scene(w.scene)
+    spec = scenes.SPECS[w.scene]
+    scene = scenes.make_scene(spec, nodes=host_nodes or spec.n_points < scenes.GPU_BUILD_POINTS)
     views = scenes.workload_views(w)
-    character = scenes.make_character(w.character) if w.character else None
+    character = scenes.make_character(w.character, root=w.character_root) if w.character else None
     return w, scene, views, character, time.time() - t
 
 
@@ -280,7 +283,7 @@ def run_gpu(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    w, scene, views, character, prep_s = prepare(WORKLOAD)
+    w, scene, views, character, prep_s = prepare(WORKLOAD, host_nodes=False)
 
     ctx = qb.OctreeGLC(local)
     # a dedicated stream: the library and the timing events must share it
@@ -290,7 +293,13 @@ def run_gpu(args):
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     ctx.upload_model(False, scene.colors, scene.normals)
-    ctx.upload_octree(False, scene.nodes)
+    if scene.nodes is not None:
+        ctx.upload_octree(False, scene.nodes)
+        n_nodes = int(scene.nodes.shape[0])
+    else:
+        # octree_insert_point numbering, built on the GPU
+        n_nodes = ctx.build_tree(False, scene.points, scene.spec.basesize, scene.spec.levels)
+        torch.cuda.synchronize()
     if args.service_min:
         ctx.set_option(qb._lib.OPT_SERVICE_MIN, args.service_min)
     if args.tile_width:
@@ -363,7 +372,10 @@ def run_gpu(args):
         # tuning options (service threshold, warp tile, blocks per SM) picked
         # by timing this frame; untimed
         update(0)
-        tuning = ctx.autotune(views, outs, reps=3, **(mlp_kw if training is not None else {}))
+        # very large frames: tune on the first views (same sizes and scene)
+        k = len(views) if sum(v.width_px * v.height_px for v in views) <= 40_000_000 else 4
+        tuning = ctx.autotune(views[:k], outs[:k], reps=3, **(mlp_kw if training is not None else {}))
+        tuning["views_timed"] = k
         torch.cuda.synchronize()
 
     use_graph = args.graph and chars is None
@@ -489,14 +501,14 @@ def run_gpu(args):
         "metric": "primary+shadow Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-        "config": {"workload": WORKLOAD, "points": int(scene.points.shape[0]), "nodes": int(scene.nodes.shape[0]),
+        "config": {"workload": WORKLOAD, "points": int(scene.points.shape[0]), "nodes": n_nodes,
                    "resolution": f"{w.width}x{w.height}" if w.width else "mixed", "views": len(views), "depth": 12,
                    "basecube": 1800.0, "rays_per_step": rays, "nominal_2wh_rays_per_step": 2 * pixels,
                    "dynamic_points": int(w.character),
                    "per_step": "re-skin + rebuild dynamic tree + render" if chars else "render",
                    "dynamic_update_ms": update_ms,
                    "l2": "flushed between steps (2x L2 write, outside the timed events); node arrays "
-                         f"{scene.nodes.shape[0] * 36 / 1e9:.2f} GB > L2",
+                         f"{n_nodes * 36 / 1e9:.2f} GB > L2",
                    "parallelism": "replicas only" if world > 1 else "single GPU",
                    "prep_seconds": round(prep_s, 1)},
         "e2e": e2e,
@@ -515,6 +527,8 @@ def run_gpu(args):
     for g in graphs:
         g.close()
     if rank == 0 and not args.no_cpu_baseline:
+        if scene.nodes is None:
+            scene.nodes = ctx.download_tree(False)  # the GPU-built tree, for the host oracle
         line["cpu_baseline"] = {k: v for k, v in cpu_sample(scene, views, budget_s=args.cpu_seconds,
                                                             character=character, frame=args.warmup).items()
                                 if k not in ("seconds", "rays")}

@@ -502,6 +502,7 @@ int qbc_octree_nodes(qbc_octree* tree, const int32_t** nodes, int64_t* n_nodes);
 
 #define QBC_SCENE_FLOOR 0 /* floor plane + boxes + spheres */
 #define QBC_SCENE_ROOM 1  /* closed room (floor, 4 walls, ceiling) + boxes + spheres */
+#define QBC_SCENE_HOUSE 2 /* 3 floors x 6 closed rooms; each box / sphere in a seeded room */
 
 typedef struct qbc_scene_desc
 {

@@ -33,6 +33,7 @@ PX_OOB = 1 << 7
 
 SCENE_FLOOR = 0
 SCENE_ROOM = 1
+SCENE_HOUSE = 2
 
 ERRORS = {-1: "QBC_E_ARG", -2: "QBC_E_CUDA", -3: "QBC_E_NOMEM", -4: "QBC_E_STATE", -5: "QBC_E_TIMEOUT", -6: "QBC_E_IO"}
 

@@ -501,30 +501,80 @@ extern "C" int qbc_scene_generate(const qbc_scene_desc* d, float* pnts, float* n
       float o[3] = {m, m, S - m}, u[3] = {w, 0, 0}, v[3] = {0, h, 0}, n[3] = {0, 0, -1};
       rect(prims, o, u, v, n, c);  // front wall
     }
+  } else if (d->kind == QBC_SCENE_HOUSE) {
+    // 3 floors of 3 x 2 closed rooms (floor, ceiling, 4 walls each)
+    const float m = 0.02f * S, fh = (S - 2.0f * m) / 3.0f, rw = (S - 2.0f * m) / 3.0f, rd = (S - 2.0f * m) / 2.0f;
+    for (int f = 0; f < 3; ++f)
+      for (int rx = 0; rx < 3; ++rx)
+        for (int rz = 0; rz < 2; ++rz) {
+          const float x0 = m + rx * rw, y0 = m + f * fh, z0 = m + rz * rd;
+          float c[3];
+          color(c);
+          {
+            float o[3] = {x0, y0, z0}, u[3] = {rw, 0, 0}, v[3] = {0, 0, rd}, n[3] = {0, 1, 0};
+            rect(prims, o, u, v, n, c);  // floor
+          }
+          {
+            float o[3] = {x0, y0 + fh, z0}, u[3] = {rw, 0, 0}, v[3] = {0, 0, rd}, n[3] = {0, -1, 0};
+            rect(prims, o, u, v, n, c);  // ceiling
+          }
+          color(c);
+          {
+            float o[3] = {x0, y0, z0}, u[3] = {0, fh, 0}, v[3] = {0, 0, rd}, n[3] = {1, 0, 0};
+            rect(prims, o, u, v, n, c);
+          }
+          {
+            float o[3] = {x0 + rw, y0, z0}, u[3] = {0, fh, 0}, v[3] = {0, 0, rd}, n[3] = {-1, 0, 0};
+            rect(prims, o, u, v, n, c);
+          }
+          {
+            float o[3] = {x0, y0, z0}, u[3] = {rw, 0, 0}, v[3] = {0, fh, 0}, n[3] = {0, 0, 1};
+            rect(prims, o, u, v, n, c);
+          }
+          {
+            float o[3] = {x0, y0, z0 + rd}, u[3] = {rw, 0, 0}, v[3] = {0, fh, 0}, n[3] = {0, 0, -1};
+            rect(prims, o, u, v, n, c);
+          }
+        }
   } else {
     return fail(QBC_E_ARG, "qbc_scene_generate: unknown scene kind %d", d->kind);
   }
   (void)lo;
 
+  // where boxes and spheres go: the single room (floor / room scenes, x and z
+  // share bounds), or a seeded room of the house
+  auto room_bounds = [&](float* b) {  // x0 x1 y0 y1 z0 z1
+    if (d->kind != QBC_SCENE_HOUSE) {
+      b[0] = xlo, b[1] = xhi, b[2] = floor_y, b[3] = hi_y, b[4] = xlo, b[5] = xhi;
+      return;
+    }
+    const float m = 0.02f * S, fh = (S - 2.0f * m) / 3.0f, rw = (S - 2.0f * m) / 3.0f, rd = (S - 2.0f * m) / 2.0f;
+    const int r = (int)(rng.next() % 18u), f = r / 6, rx = (r / 2) % 3, rz = r % 2;
+    b[0] = m + rx * rw, b[1] = b[0] + rw, b[2] = m + f * fh, b[3] = b[2] + fh, b[4] = m + rz * rd, b[5] = b[4] + rd;
+  };
   for (int b = 0; b < d->n_boxes; ++b) {
+    float rb[6];
+    room_bounds(rb);
     float sx = rng.range(d->box_min, d->box_max);
     float sy = rng.range(d->box_min, d->box_max);
     float sz = rng.range(d->box_min, d->box_max);
-    sx = std::min(sx, 0.9f * (xhi - xlo));
-    sz = std::min(sz, 0.9f * (xhi - xlo));
-    sy = std::min(sy, 0.9f * (hi_y - floor_y));
-    float x0 = rng.range(xlo, xhi - sx);
-    float z0 = rng.range(xlo, xhi - sz);
+    sx = std::min(sx, 0.9f * (rb[1] - rb[0]));
+    sz = std::min(sz, 0.9f * (rb[5] - rb[4]));
+    sy = std::min(sy, 0.9f * (rb[3] - rb[2]));
+    float x0 = rng.range(rb[0], rb[1] - sx);
+    float z0 = rng.range(rb[4], rb[5] - sz);
     float c[3];
     color(c);
-    box(prims, x0, floor_y, z0, sx, sy, sz, c);
+    box(prims, x0, rb[2], z0, sx, sy, sz, c);
   }
   for (int s = 0; s < d->n_spheres; ++s) {
+    float rb[6];
+    room_bounds(rb);
     float r = rng.range(d->sphere_min, d->sphere_max);
-    r = std::min(r, 0.45f * std::min(xhi - xlo, hi_y - floor_y));
-    float cx = rng.range(xlo + r, xhi - r);
-    float cy = rng.range(floor_y + r, hi_y - r);
-    float cz = rng.range(xlo + r, xhi - r);
+    r = std::min(r, 0.45f * std::min(std::min(rb[1] - rb[0], rb[5] - rb[4]), rb[3] - rb[2]));
+    float cx = rng.range(rb[0] + r, rb[1] - r);
+    float cy = rng.range(rb[2] + r, rb[3] - r);
+    float cz = rng.range(rb[4] + r, rb[5] - r);
     float c[3];
     color(c);
     sphere(prims, cx, cy, cz, r, c);

@@ -67,6 +67,10 @@ SPECS = {
 # the room scene at a quarter of the points: a profiling case whose node
 # arrays (~0.5 GB) still exceed L2 but keep an ncu capture short
 SPECS["room5m"] = SceneSpec(_lib.SCENE_ROOM, 5_000_000, 2, 200, (20.0, 300.0), 100, (10.0, 150.0), 0.05)
+# house scale: 3 floors x 6 rooms, 40 boxes and 20 spheres per room on average
+SPECS["house90m"] = SceneSpec(_lib.SCENE_HOUSE, 90_000_000, 5, 720, (20.0, 300.0), 360, (10.0, 150.0), 0.05)
+# scenes this large are built on the GPU (qbc_build_tree), not by the host producer
+GPU_BUILD_POINTS = 30_000_000
 
 
 @dataclass
@@ -91,12 +95,15 @@ def generate_points(spec: SceneSpec):
     return pts, nrm, col
 
 
-def make_scene(spec) -> Scene:
+def make_scene(spec, nodes: bool = True) -> Scene:
+    """Points, attributes and (unless nodes is False) the host-built node
+    array of a spec; without nodes, Scene.nodes is None and the caller builds
+    the tree on the GPU from Scene.points."""
     if isinstance(spec, str):
         spec = SPECS[spec]
     pts, nrm, col = generate_points(spec)
-    nodes = build_octree(pts, spec.basesize, spec.levels)
-    return Scene(spec, pts, nrm, col, nodes)
+    arr = build_octree(pts, spec.basesize, spec.levels) if nodes else None
+    return Scene(spec, pts, nrm, col, arr)
 
 
 def scaled_spec(name: str, n_points: int) -> SceneSpec:
@@ -173,6 +180,7 @@ class Workload:
     fov_deg: float = 60.0
     sizes: List = None        # per-view (width, height) when views differ in size
     character: int = 0        # points of a dynamic character re-skinned every frame
+    character_root: tuple = (900.0, 500.0, 1100.0)
     train_poses: List = None  # poses whose plain shadow walks train the occluder-proposal network
     train_size: tuple = (960, 720)
 
@@ -212,6 +220,21 @@ WORKLOADS["floor1m_char2m_mixed_x64"] = Workload("floor1m_char2m_mixed_x64", "fl
 # (about 10^7 logged shadow rays), 16 held-out poses at 1920x1080
 WORKLOADS["floor1m_mlp_1920x1080x16"] = Workload("floor1m_mlp_1920x1080x16", "floor1m", 1920, 1080,
                                                  batch_views(3002, 16)[1], train_poses=batch_views(3001, 256)[1])
+
+
+# house scale: 32 poses on a seeded spline through the ground floor at
+# 3840x2160, a 10M-point character standing in a ground-floor room
+WORKLOADS["house90m_char10m_3840x2160x32"] = Workload(
+    "house90m_char10m_3840x2160x32", "house90m", 3840, 2160,
+    spline_poses(1005, 32, lo=(120.0, 150.0, 120.0), hi=(1680.0, 480.0, 1680.0)), character=10_000_000,
+    character_root=(900.0, 40.0, 500.0))
+# the same frame with the occluder-proposal network retrained on this scene
+# (256 training poses of another ground-floor spline at 960x720)
+WORKLOADS["house90m_char10m_mlp_3840x2160x32"] = Workload(
+    "house90m_char10m_mlp_3840x2160x32", "house90m", 3840, 2160,
+    spline_poses(1005, 32, lo=(120.0, 150.0, 120.0), hi=(1680.0, 480.0, 1680.0)), character=10_000_000,
+    character_root=(900.0, 40.0, 500.0),
+    train_poses=spline_poses(1006, 256, lo=(120.0, 150.0, 120.0), hi=(1680.0, 480.0, 1680.0)))
 
 
 def train_views(w: Workload, maxlevel: int = LEVELS, basesize: float = BASESIZE):

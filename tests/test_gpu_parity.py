@@ -122,6 +122,24 @@ def test_dynamic_tree_frame(ctx, oracle, floor50k_scene):
     assert stats["primary_leaf"] > 1000
 
 
+def test_house_scene_with_character(ctx, oracle):
+    """The house scene (3 floors x 6 closed rooms) at 2M points with the
+    bone-chain character in a ground-floor room, from the house workload's
+    first poses at reduced size: every stream bit-exact."""
+    from qubatron_gb300 import build_octree, scenes, view_setup
+    s = scenes.make_scene(scenes.scaled_spec("house90m", 2_000_000))
+    w = scenes.WORKLOADS["house90m_char10m_3840x2160x32"]
+    ch = scenes.make_character(60_000, root=w.character_root)
+    p, n = scenes.skin_reference(ch, scenes.pose_bones(ch, 2))
+    dnodes = build_octree(p, S, LEVELS)
+    upload_scene(ctx, s.nodes, s.colors, s.normals, dnodes, ch.colors, n)
+    sc = oracle_scene(oracle, s.nodes, s.colors, s.normals, dnodes, ch.colors, n)
+    for pos, ang in w.poses[:3]:
+        v = view_setup(384, 216, pos, ang, 0.0, 10, LEVELS, S, 0, scenes.vertical_fov_focal(216))
+        stats = compare_frame(gpu_frame(ctx, v), oracle.render(sc, _view_for_oracle(oracle, v)), f"house {pos}")
+        assert stats["primary_leaf"] > 500
+
+
 def test_inexact_basesize_uses_replay(ctx, oracle):
     """A basecube edge whose cube coordinates are not all representable:
     the cube of a level is then replayed from the root instead of undone."""
