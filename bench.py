@@ -349,6 +349,8 @@ def run_gpu(args):
                     "collect_s": round(collect_s, 2), "train_s": round(time.time() - t0, 2),
                     "gate_per_mille": args.proposal_gate, "proposal_level": args.proposal_level}
         ctx.set_option(qb._lib.OPT_PROPOSAL_GATE, args.proposal_gate)
+        ctx.set_option(qb._lib.OPT_PROPOSAL_COUNT, args.proposal_count)
+        training["proposal_count"] = args.proposal_count
         render = render_mlp
 
     # device outputs
@@ -560,6 +562,7 @@ def main():
                     help="time eager launches instead of CUDA graph replays of the frame")
     ap.add_argument("--proposal-gate", type=int, default=500, help="occlusion probability (per mille) to try")
     ap.add_argument("--proposal-level", type=int, default=8, help="octree level of the proposed cells")
+    ap.add_argument("--proposal-count", type=int, default=3, help="network proposals tried per pixel (1..3)")
     args = ap.parse_args()
     global WORKLOAD
     if args.workload:

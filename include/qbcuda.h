@@ -441,6 +441,8 @@ int qbc_synchronize(qbc_ctx* ctx);
  *   QBC_OPT_PROPOSAL_GATE  0..999 per mille, default 500: QBC_PROPOSE_MLP
  *   tries a pixel's proposals only when the network's occlusion probability
  *   is at least this (0: always).
+ *   QBC_OPT_PROPOSAL_COUNT  1..3, default 3: network proposals tried per
+ *   pixel, earliest first.
  *   QBC_OPT_TILE_WIDTH  4, 8 (default), 16 or 32: width of the 32-pixel warp
  *   tiles the render kernels take from their queue (height 32 / width).
  *   QBC_OPT_BLOCKS_PER_SM  0 (default: as many as fit) .. 32: resident
@@ -450,6 +452,7 @@ int qbc_synchronize(qbc_ctx* ctx);
 #define QBC_OPT_PROPOSAL_GATE 2
 #define QBC_OPT_TILE_WIDTH 3
 #define QBC_OPT_BLOCKS_PER_SM 4
+#define QBC_OPT_PROPOSAL_COUNT 5
 int qbc_set_option(qbc_ctx* ctx, int option, int value);
 int qbc_get_option(qbc_ctx* ctx, int option, int* value);
 

@@ -248,6 +248,7 @@ OPT_SERVICE_MIN = 1
 OPT_PROPOSAL_GATE = 2
 OPT_TILE_WIDTH = 3
 OPT_BLOCKS_PER_SM = 4
+OPT_PROPOSAL_COUNT = 5
 
 
 def lib_path() -> str:

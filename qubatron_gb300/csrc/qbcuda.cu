@@ -96,6 +96,7 @@ struct qbc_ctx {
   int tile_shift = 3;     // 8x4 warp tiles
   int blocks_per_sm = 0;  // render blocks per SM (0: as many as fit)
   int proposal_gate = 500;  // per mille: minimum predicted occlusion probability to try a proposal
+  int proposal_count = 3;   // network proposals tried per pixel (earliest first)
   int64_t launches = 0;
 };
 
@@ -237,6 +238,11 @@ extern "C" int qbc_set_option(qbc_ctx* c, int option, int value) {
     c->proposal_gate = value;
     return QBC_OK;
   }
+  if (option == QBC_OPT_PROPOSAL_COUNT) {
+    if (value < 1 || value > 3) return fail(QBC_E_ARG, "qbc_set_option: proposal count %d outside 1..3", value);
+    c->proposal_count = value;
+    return QBC_OK;
+  }
   if (option == QBC_OPT_TILE_WIDTH) {
     if (value != 4 && value != 8 && value != 16 && value != 32)
       return fail(QBC_E_ARG, "qbc_set_option: tile width %d (4, 8, 16 or 32)", value);
@@ -259,6 +265,10 @@ extern "C" int qbc_get_option(qbc_ctx* c, int option, int* value) {
   }
   if (option == QBC_OPT_PROPOSAL_GATE) {
     *value = c->proposal_gate;
+    return QBC_OK;
+  }
+  if (option == QBC_OPT_PROPOSAL_COUNT) {
+    *value = c->proposal_count;
     return QBC_OK;
   }
   if (option == QBC_OPT_TILE_WIDTH) {
@@ -740,6 +750,7 @@ struct RecordRows {
   qbc::Batch b;
   qbc::Wave w;
   float gate;
+  int keep;  // proposals kept, earliest first
   __device__ __forceinline__ uint32_t rows() const { return min(*w.qcount, w.cap); }
   __device__ __forceinline__ void load(uint32_t r0, uint32_t n, bf16* x, int lane) const {
     if (lane >= 16) return;
@@ -760,6 +771,7 @@ struct RecordRows {
           t[i] = t[j];
           t[j] = x;
         }
+    for (int k = keep; k < 3; ++k) t[k] = -1.0f;
     uint32_t* rec = w.rec + (size_t)r * qbc::kRecWords;
     for (int k = 0; k < 3; ++k) rec[qbc::kRecProp + k] = __float_as_uint(t[k]);
   }
@@ -845,6 +857,7 @@ int propose_mlp(qbc_ctx* c, const qbc::Batch& b, const qbc::Wave& w) {
   src->w = w;
   const float p = (float)c->proposal_gate * 1e-3f;  // gate probability -> logit
   src->gate = c->proposal_gate <= 0 ? -INFINITY : logf(p / (1.0f - p));
+  src->keep = c->proposal_count;
   return launch_fused(c, *src, 0);
 }
 
@@ -1156,6 +1169,7 @@ struct FrameSignature {
   int32_t proposal_gate;
   int32_t tile_shift;
   int32_t blocks_per_sm;
+  int32_t proposal_count;
 };
 
 bool same_signature(const FrameSignature& a, const FrameSignature& b) {
@@ -1167,7 +1181,8 @@ bool same_signature(const FrameSignature& a, const FrameSignature& b) {
   }
   return a.rec == b.rec && a.rec_cap == b.rec_cap && a.pixlog == b.pixlog && a.pixlog_cap == b.pixlog_cap &&
          a.net_w == b.net_w && a.net_b == b.net_b && a.stream == b.stream && a.service_min == b.service_min &&
-         a.proposal_gate == b.proposal_gate && a.tile_shift == b.tile_shift && a.blocks_per_sm == b.blocks_per_sm;
+         a.proposal_gate == b.proposal_gate && a.tile_shift == b.tile_shift && a.blocks_per_sm == b.blocks_per_sm &&
+         a.proposal_count == b.proposal_count;
 }
 
 FrameSignature frame_signature(const qbc_ctx* c) {
@@ -1184,6 +1199,7 @@ FrameSignature frame_signature(const qbc_ctx* c) {
   f.proposal_gate = c->proposal_gate;
   f.tile_shift = c->tile_shift;
   f.blocks_per_sm = c->blocks_per_sm;
+  f.proposal_count = c->proposal_count;
   return f;
 }
 
