@@ -267,16 +267,18 @@ def measure_e2e(ctx, views, rays, world, flush, steps, update=None, render=None)
             update(k)
         render(views, houts, False)
         e2e_t.append(time.perf_counter() - t0)
-    e2e_s = statistics.mean(e2e_t)
+    from qubatron_gb300 import replicas
+    rate, slowest_s = replicas.job_throughput(rays * len(e2e_t), sum(e2e_t), device="cuda")
     d2h = sum(h.numel() for h in host)
     h2d = len(views) * 132  # qbc_view uniforms, passed as launch parameters
-    return {"value": world * rays / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
-            "d2h_bytes_per_step": d2h, "ms_per_step": 1000.0 * e2e_s}
+    return {"value": rate / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h, "ms_per_step": 1000.0 * slowest_s / len(e2e_t)}
 
 
 def run_gpu(args):
     import torch
     import qubatron_gb300 as qb
+    from qubatron_gb300 import replicas
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
@@ -425,8 +427,7 @@ def run_gpu(args):
         torch.cuda.synchronize()
         l0 = ctx.launch_count()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-        if world > 1:
-            torch.distributed.barrier()
+        replicas.barrier()
         torch.cuda.synchronize()
         with ClockSampler(local) as clk:
             for k in range(args.steps):
@@ -436,17 +437,15 @@ def run_gpu(args):
                 render_fn(views, outs, True)
                 ev[k][1].record(stream)
             torch.cuda.synchronize()
-        if world > 1:
-            torch.distributed.barrier()
+        replicas.barrier()
         return [a.elapsed_time(b) for a, b in ev], ctx.launch_count() - l0, clk
 
     step_ms, launches, clk = timed(render)
-    ms = statistics.mean(step_ms)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * sum(frame_rays) / (sum(step_ms) / 1000.0) / 1e6
+    # replicas: every rank renders the whole workload; the job's throughput
+    # is all ranks' rays over the slowest rank's time
+    rate, slowest_s = replicas.job_throughput(sum(frame_rays), sum(step_ms) / 1000.0, device="cuda")
+    value = rate / 1e6
+    ms = 1000.0 * slowest_s / len(step_ms)
 
     proposal = None
     if training is not None:
