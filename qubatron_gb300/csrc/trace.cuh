@@ -117,12 +117,22 @@ __device__ __forceinline__ float4 parent_cube(float4 t, int o) {
   return t;
 }
 
-// Point of candidate source src (1 z, 2 x, 3 y bisecting plane) of cube t.
+// Point of candidate source src (1 z, 2 x, 3 y bisecting plane) of cube t:
+// hit_{z,x,y}plane of the cube's midpoint, as one plane hit whose axis is
+// picked by selects (the same operations on the same operands, so the same
+// bits), because lanes of a warp pop to candidates of different sources.
 __device__ __forceinline__ float4 plane_point(int src, float4 t, float3 p, float3 d) {
-  float3 h = hlf_of(t);
-  if (src == 1) return hit_zplane(h.z, p, d);
-  if (src == 2) return hit_xplane(h.x, p, d);
-  return hit_yplane(h.y, p, d);
+  const float3 h = hlf_of(t);
+  const bool ax = src == 2, ay = src == 3;
+  const float c = ax ? h.x : (ay ? h.y : h.z);
+  const float pa = ax ? p.x : (ay ? p.y : p.z);
+  const float da = ax ? d.x : (ay ? d.y : d.z);
+  const bool par = da == 0.0f;
+  const float w = (c - pa) / (par ? 1.0f : da);
+  const float x = ax ? c : p.x + d.x * w;
+  const float y = ay ? c : p.y + d.y * w;
+  const float z = (ax | ay) ? p.z + d.z * w : c;
+  return make_float4(par ? kFltMax : x, par ? kFltMax : y, par ? kFltMax : z, par ? kFltMax : w);
 }
 
 __device__ __forceinline__ int32_t pick8(int4 a, int4 b, int o) {

@@ -129,41 +129,22 @@ struct Walker {
     uint32_t c[4];
     t[0] = e.w;
     c[0] = (e.x > hl.x ? 1u : 0u) | (e.y < hl.y ? 2u : 0u) | (e.z < hl.z ? 4u : 0u);
-    t[1] = t[2] = t[3] = kInf;
-    c[1] = c[2] = c[3] = 0u;
-    int hc = 1;
-    if (vz) {
-      t[1] = hz.w;
-      c[1] = (hz.x > hl.x ? 1u : 0u) | (hz.y < hl.y ? 2u : 0u) | (1u << 3);
-      hc = 2;
+    {
+      // the valid plane hits fill slots 1.. in the order z, x, y (selects:
+      // the lanes of a warp differ in which hits are valid)
+      const uint32_t cz = (hz.x > hl.x ? 1u : 0u) | (hz.y < hl.y ? 2u : 0u) | (1u << 3);
+      const uint32_t cx = (hx.y < hl.y ? 2u : 0u) | (hx.z < hl.z ? 4u : 0u) | (2u << 3);
+      const uint32_t cy = (hy.x > hl.x ? 1u : 0u) | (hy.z < hl.z ? 4u : 0u) | (3u << 3);
+      t[1] = vz ? hz.w : (vx ? hx.w : (vy ? hy.w : kInf));
+      c[1] = vz ? cz : (vx ? cx : (vy ? cy : 0u));
+      const bool s2x = vz & vx, s2y = !s2x & (vz | vx) & vy;
+      t[2] = s2x ? hx.w : (s2y ? hy.w : kInf);
+      c[2] = s2x ? cx : (s2y ? cy : 0u);
+      const bool s3 = vz & vx & vy;
+      t[3] = s3 ? hy.w : kInf;
+      c[3] = s3 ? cy : 0u;
     }
-    if (vx) {
-      float tv = hx.w;
-      uint32_t cv = (hx.y < hl.y ? 2u : 0u) | (hx.z < hl.z ? 4u : 0u) | (2u << 3);
-      if (hc == 1) {
-        t[1] = tv;
-        c[1] = cv;
-      } else {
-        t[2] = tv;
-        c[2] = cv;
-      }
-      ++hc;
-    }
-    if (vy) {
-      float tv = hy.w;
-      uint32_t cv = (hy.x > hl.x ? 1u : 0u) | (hy.z < hl.z ? 4u : 0u) | (3u << 3);
-      if (hc == 1) {
-        t[1] = tv;
-        c[1] = cv;
-      } else if (hc == 2) {
-        t[2] = tv;
-        c[2] = cv;
-      } else {
-        t[3] = tv;
-        c[3] = cv;
-      }
-      ++hc;
-    }
+    const int hc = 1 + (int)vz + (int)vx + (int)vy;
     // ordering by swaps, as the shader's nested loop (:276-290)
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
