@@ -13,6 +13,16 @@
 //           length in bits 20-22, next index in bits 23-25;
 //   word 1  the level's static node index;
 //   word 2  the level's dynamic node index (only with a dynamic tree).
+//
+// With EXACT (every cube coordinate representable: basecube (0, S, S, S) and
+// the odd part of S has at most 24 - maxlevel bits) the current cube is not
+// kept as floats but as its path: X, Y, Z hold one bit per level (the octet's
+// x, y, z shift bits, root first), so the cube of level L is exactly
+// (X * u, S - Y * u, S - Z * u, u) with u = S / 2^L, the same values the
+// shader's successive halvings and shifts produce. A bit mask `more` marks
+// the levels whose candidate lists have unused entries, so a pop jumps to
+// its level in constant time (highest set bit, shift the path right) instead
+// of walking up level by level.
 #pragma once
 
 #include "trace.cuh"
@@ -25,7 +35,9 @@ template <bool EXACT, bool DYN, bool PROP = false>
 struct Walker {
   float3 p, d;   // ray origin and direction
   float4 e0;     // entry point of the basecube
-  float4 cube;   // current cube (tlf.xyz, edge)
+  float4 cube;   // current cube (tlf.xyz, edge); !EXACT only
+  uint32_t X, Y, Z;  // EXACT: path shift bits of the current cube, one per level
+  uint32_t more;     // EXACT: bit L set when level L's candidate list has unused entries
   float4 e;      // entry point of the current cube
   int level;
   int32_t ns, nd;
@@ -44,11 +56,20 @@ struct Walker {
     return st.base[(kWords * l + k) * st.stride];
   }
 
+  // Cube of the current level from the path (EXACT): exact products and
+  // sums, so equal to the successive child shifts.
+  __device__ __forceinline__ float4 cube_of_path(float4 bc) const {
+    const float u = bc.w * __int_as_float((127 - level) << 23);  // S / 2^level
+    return make_float4(bc.x + (float)X * u, bc.y - (float)Y * u, bc.z - (float)Z * u, u);
+  }
+
   // Basecube entry (octree_fsh.c:157-211). Returns kDiscard or kRunning.
   __device__ __forceinline__ int start(float4 bc, float3 rp, float3 rd) {
     p = rp;
     d = rd;
     cube = bc;
+    X = Y = Z = 0u;
+    more = 0u;
     level = 0;
     ns = 0;
     nd = 0;
@@ -103,6 +124,8 @@ struct Walker {
   // Returns kRunning, kLeaf (fields via leaf()) or kMiss.
   __device__ __forceinline__ int step(const DevScene& sc, int maxlevel, float4 bc, const Stack& st) {
     if (level == maxlevel) return kLeaf;
+
+    if (EXACT) cube = cube_of_path(bc);
 
     // ---- subnode test (octree_fsh.c:251-329) ----
     int4 s0, s1, d0, d1;
@@ -220,13 +243,27 @@ struct Walker {
       if (DYN) slot(st, level, 2) = (uint32_t)nd;
     } else {
       // ---- pop until a level has candidates left (:368-375) ----
-      for (;;) {
-        if (level == (PROP ? tdepth : 0)) return kMiss;
-        --level;
+      if (EXACT) {
+        // the nearest level above with unused candidates, in one jump
+        const uint32_t m = PROP ? (more & ~((1u << tdepth) - 1u)) : more;
+        if (m == 0u) return kMiss;
+        const int lv = 31 - __clz(m);
+        const int up = level - lv;
+        X >>= up;
+        Y >>= up;
+        Z >>= up;
+        level = lv;
         pk = slot(st, level, 0);
         nx = list_next(pk);
-        if (EXACT) cube = parent_cube(cube, list_entry(pk, nx - 1) & 7);
-        if (nx < list_len(pk)) break;
+        cube = cube_of_path(bc);
+      } else {
+        for (;;) {
+          if (level == (PROP ? tdepth : 0)) return kMiss;
+          --level;
+          pk = slot(st, level, 0);
+          nx = list_next(pk);
+          if (nx < list_len(pk)) break;
+        }
       }
       cc = list_entry(pk, nx);
       int src = cc >> 3;
@@ -249,7 +286,14 @@ struct Walker {
       return kMiss;
     }
     slot(st, level, 0) = (pk & ~(7u << 23)) | ((uint32_t)(nx + 1) << 23);
-    cube = child_cube(cube, cc & 7);
+    if (EXACT) {
+      more = (more & ~(1u << level)) | (nx + 1 < list_len(pk) ? (1u << level) : 0u);
+      X = (X << 1) | (uint32_t)(cc & 1);
+      Y = (Y << 1) | (uint32_t)((cc >> 1) & 1);
+      Z = (Z << 1) | (uint32_t)((cc >> 2) & 1);
+    } else {
+      cube = child_cube(cube, cc & 7);
+    }
     e = isp;
     ns = cs;
     nd = cd;
