@@ -74,6 +74,23 @@ __device__ __forceinline__ float4 hit_zplane(float z, float3 p, float3 d) {
                      par ? kFltMax : w);
 }
 
+// The same plane hits without the parallel-ray sentinel: for a ray parallel
+// to the plane the values are meaningless and the caller must treat the hit
+// as invalid (the sentinel only ever makes the face test fail). Non-parallel
+// rays get exactly the values above.
+__device__ __forceinline__ float4 hit_xplane_raw(float x, float3 p, float3 d) {
+  const float w = (x - p.x) / (d.x == 0.0f ? 1.0f : d.x);
+  return make_float4(x, p.y + d.y * w, p.z + d.z * w, w);
+}
+__device__ __forceinline__ float4 hit_yplane_raw(float y, float3 p, float3 d) {
+  const float w = (y - p.y) / (d.y == 0.0f ? 1.0f : d.y);
+  return make_float4(p.x + d.x * w, y, p.z + d.z * w, w);
+}
+__device__ __forceinline__ float4 hit_zplane_raw(float z, float3 p, float3 d) {
+  const float w = (z - p.z) / (d.z == 0.0f ? 1.0f : d.z);
+  return make_float4(p.x + d.x * w, p.y + d.y * w, z, w);
+}
+
 // Half-open face tests (octree_fsh.c:166-192, 263-271), evaluated without
 // short-circuit branches.
 __device__ __forceinline__ bool in_zface(float4 a, float4 t, float4 b) {

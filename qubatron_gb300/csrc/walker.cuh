@@ -135,12 +135,14 @@ struct Walker {
     }
     float4 cb = brb_of(cube);
     float3 hl = hlf_of(cube);
-    float4 hz = hit_zplane(hl.z, p, d);
-    float4 hx = hit_xplane(hl.x, p, d);
-    float4 hy = hit_yplane(hl.y, p, d);
-    bool vz = hz.w > 0.0f && in_zface(hz, cube, cb);
-    bool vx = hx.w > 0.0f && in_xface(hx, cube, cb);
-    bool vy = hy.w > 0.0f && in_yface(hy, cube, cb);
+    // a ray parallel to a bisecting plane has no hit on it (the shader's
+    // FLT_MAX sentinel fails the face test)
+    float4 hz = hit_zplane_raw(hl.z, p, d);
+    float4 hx = hit_xplane_raw(hl.x, p, d);
+    float4 hy = hit_yplane_raw(hl.y, p, d);
+    bool vz = (d.z != 0.0f) & (hz.w > 0.0f) & in_zface(hz, cube, cb);
+    bool vx = (d.x != 0.0f) & (hx.w > 0.0f) & in_xface(hx, cube, cb);
+    bool vy = (d.y != 0.0f) & (hy.w > 0.0f) & in_yface(hy, cube, cb);
 
     // Candidates in the shader's fill order (entry, z, x, y), compacted, as
     // (t, code): code = octet side bits | source << 3. A bisecting-plane hit
@@ -298,7 +300,9 @@ struct Walker {
     ns = cs;
     nd = cd;
     ++level;
-    return kRunning;
+    // a descent into the last level is the leaf hit (the loop's next pass
+    // would return it before any subnode test, octree_fsh.c:218)
+    return level == maxlevel ? kLeaf : kRunning;
   }
 
   // Leaf fetch (octree_fsh.c:218-247); call after step() returned kLeaf.
