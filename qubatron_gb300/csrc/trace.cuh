@@ -74,6 +74,40 @@ __device__ __forceinline__ float4 hit_zplane(float z, float3 p, float3 d) {
                      par ? kFltMax : w);
 }
 
+// Correctly rounded a / b from y = RN(1 / b), by Markstein's method (P.
+// Markstein, "Computation of elementary functions on the IBM RISC System/6000
+// processor", IBM J. Res. Develop. 34(1), 1990; proofs in M. Cornea-Hasegan,
+// R. Golliver, P. Markstein, "Correctness proofs outline for Newton-Raphson
+// based floating-point divide and square root algorithms", ARITH 14, 1999):
+// if y is within half an ulp of 1/b and q within one ulp of a/b, the
+// remainder r = a - b q is exact in one FMA and RN(q + r y) = RN(a / b).
+// q0 = RN(a y) is within 1.5 ulp, the first correction brings it within one
+// ulp, the second rounds correctly. Valid when nothing overflows or
+// underflows; callers use it only for rays whose magnitudes rule that out
+// (recip_div_ok), and a test checks it against IEEE division.
+__device__ __forceinline__ float div_by_recip(float a, float b, float y) {
+  float q = __fmul_rn(a, y);
+  float r = __fmaf_rn(-b, q, a);
+  q = __fmaf_rn(r, y, q);
+  r = __fmaf_rn(-b, q, a);
+  return __fmaf_rn(r, y, q);
+}
+
+// Whether div_by_recip is exact for every plane hit of a ray from p along d
+// in a cube of edge S (numerators c - p with c a cube coordinate or midpoint
+// in (0, 2S], so |a| is 0 or within [2^-63, 2^66]): quotients and remainders
+// then stay normal. A zero direction component is fine (that plane is never
+// hit).
+__device__ __forceinline__ bool recip_div_ok(float3 p, float3 d, float S) {
+  auto dir_ok = [](float v) {
+    const float a = fabsf(v);
+    return (a == 0.0f) | ((a >= 9.094947e-13f) & (a <= 1.0995116e12f));  // 2^-40 .. 2^40
+  };
+  auto pos_ok = [](float v) { return fabsf(v) <= 1.8446744e19f; };  // 2^64
+  return dir_ok(d.x) & dir_ok(d.y) & dir_ok(d.z) & pos_ok(p.x) & pos_ok(p.y) & pos_ok(p.z) &
+         (S >= 9.536743e-07f) & (S <= 1.0995116e12f);  // 2^-20 .. 2^40
+}
+
 // The same plane hits without the parallel-ray sentinel: for a ray parallel
 // to the plane the values are meaningless and the caller must treat the hit
 // as invalid (the sentinel only ever makes the face test fail). Non-parallel
@@ -88,6 +122,20 @@ __device__ __forceinline__ float4 hit_yplane_raw(float y, float3 p, float3 d) {
 }
 __device__ __forceinline__ float4 hit_zplane_raw(float z, float3 p, float3 d) {
   const float w = (z - p.z) / (d.z == 0.0f ? 1.0f : d.z);
+  return make_float4(p.x + d.x * w, p.y + d.y * w, z, w);
+}
+
+// Plane hits with the division by reciprocal (rays where recip_div_ok).
+__device__ __forceinline__ float4 hit_xplane_rcp(float x, float3 p, float3 d, float y) {
+  const float w = div_by_recip(x - p.x, d.x, y);
+  return make_float4(x, p.y + d.y * w, p.z + d.z * w, w);
+}
+__device__ __forceinline__ float4 hit_yplane_rcp(float yv, float3 p, float3 d, float y) {
+  const float w = div_by_recip(yv - p.y, d.y, y);
+  return make_float4(p.x + d.x * w, yv, p.z + d.z * w, w);
+}
+__device__ __forceinline__ float4 hit_zplane_rcp(float z, float3 p, float3 d, float y) {
+  const float w = div_by_recip(z - p.z, d.z, y);
   return make_float4(p.x + d.x * w, p.y + d.y * w, z, w);
 }
 
@@ -150,6 +198,22 @@ __device__ __forceinline__ float4 plane_point(int src, float4 t, float3 p, float
   const float y = ay ? c : p.y + d.y * w;
   const float z = (ax | ay) ? p.z + d.z * w : c;
   return make_float4(par ? kFltMax : x, par ? kFltMax : y, par ? kFltMax : z, par ? kFltMax : w);
+}
+
+// plane_point with the division by reciprocal (a valid candidate: its ray is
+// not parallel to the plane). yr = RN(1 / d) per component.
+__device__ __forceinline__ float4 plane_point_rcp(int src, float4 t, float3 p, float3 d, float3 yr) {
+  const float3 h = hlf_of(t);
+  const bool ax = src == 2, ay = src == 3;
+  const float c = ax ? h.x : (ay ? h.y : h.z);
+  const float pa = ax ? p.x : (ay ? p.y : p.z);
+  const float da = ax ? d.x : (ay ? d.y : d.z);
+  const float ya = ax ? yr.x : (ay ? yr.y : yr.z);
+  const float w = div_by_recip(c - pa, da, ya);
+  const float x = ax ? c : p.x + d.x * w;
+  const float y = ay ? c : p.y + d.y * w;
+  const float z = (ax | ay) ? p.z + d.z * w : c;
+  return make_float4(x, y, z, w);
 }
 
 __device__ __forceinline__ int32_t pick8(int4 a, int4 b, int o) {

@@ -34,7 +34,9 @@ enum : int { kRunning = 3 };
 template <bool EXACT, bool DYN, bool PROP = false>
 struct Walker {
   float3 p, d;   // ray origin and direction
-  float4 e0;     // entry point of the basecube
+  float3 inv;    // EXACT: RN(1 / d) per component (0 for a zero component)
+  bool fdiv;     // EXACT: plane hits divide by reciprocal (div_by_recip)
+  float4 e0;     // entry point of the basecube (!EXACT; EXACT recomputes it)
   float4 cube;   // current cube (tlf.xyz, edge); !EXACT only
   uint32_t X, Y, Z;  // EXACT: path shift bits of the current cube, one per level
   uint32_t more;     // EXACT: bit L set when level L's candidate list has unused entries
@@ -63,7 +65,33 @@ struct Walker {
     return make_float4(bc.x + (float)X * u, bc.y - (float)Y * u, bc.z - (float)Z * u, u);
   }
 
-  // Basecube entry (octree_fsh.c:157-211). Returns kDiscard or kRunning.
+  // Basecube entry point (octree_fsh.c:157-211): false for a discard.
+  __device__ __forceinline__ bool entry(float4 bc, float4& h0) const {
+    float4 cb = brb_of(bc);
+    int hitc = 0;
+    float4 h1 = make_float4(0.f, 0.f, 0.f, 0.f), a;
+    h0 = h1;
+#define QB_FACE(expr, test)     \
+  a = expr;                     \
+  if (test) {                   \
+    if (hitc == 0) h0 = a;      \
+    else if (hitc == 1) h1 = a; \
+    ++hitc;                     \
+  }
+    QB_FACE(hit_zplane(bc.z, p, d), in_zface(a, bc, cb))  // front
+    QB_FACE(hit_zplane(cb.z, p, d), in_zface(a, bc, cb))  // back
+    QB_FACE(hit_xplane(bc.x, p, d), in_xface(a, bc, cb))  // left
+    QB_FACE(hit_xplane(cb.x, p, d), in_xface(a, bc, cb))  // right
+    QB_FACE(hit_yplane(bc.y, p, d), in_yface(a, bc, cb))  // top
+    QB_FACE(hit_yplane(cb.y, p, d), in_yface(a, bc, cb))  // bottom
+#undef QB_FACE
+    if (hitc < 2 || (h0.w < 0.0f && h1.w < 0.0f)) return false;
+    if (h1.w < h0.w) h0 = h1;
+    if (h0.w < 0.0f) h0 = make_float4(p.x, p.y, p.z, 0.0f);
+    return true;
+  }
+
+  // Start a ray: the basecube entry. Returns kDiscard or kRunning.
   __device__ __forceinline__ int start(float4 bc, float3 rp, float3 rd) {
     p = rp;
     d = rd;
@@ -79,27 +107,15 @@ struct Walker {
     vis_d = 0;
     target = 0;
     tdepth = 0;
-    float4 cb = brb_of(bc);
-    int hitc = 0;
-    float4 h0 = make_float4(0.f, 0.f, 0.f, 0.f), h1 = h0, a;
-#define QB_FACE(expr, test)     \
-  a = expr;                     \
-  if (test) {                   \
-    if (hitc == 0) h0 = a;      \
-    else if (hitc == 1) h1 = a; \
-    ++hitc;                     \
-  }
-    QB_FACE(hit_zplane(bc.z, p, d), in_zface(a, bc, cb))  // front
-    QB_FACE(hit_zplane(cb.z, p, d), in_zface(a, bc, cb))  // back
-    QB_FACE(hit_xplane(bc.x, p, d), in_xface(a, bc, cb))  // left
-    QB_FACE(hit_xplane(cb.x, p, d), in_xface(a, bc, cb))  // right
-    QB_FACE(hit_yplane(bc.y, p, d), in_yface(a, bc, cb))  // top
-    QB_FACE(hit_yplane(cb.y, p, d), in_yface(a, bc, cb))  // bottom
-#undef QB_FACE
-    if (hitc < 2 || (h0.w < 0.0f && h1.w < 0.0f)) return kDiscard;
-    if (h1.w < h0.w) h0 = h1;
-    if (h0.w < 0.0f) h0 = make_float4(p.x, p.y, p.z, 0.0f);
-    e0 = h0;
+    float4 h0;
+    if (!entry(bc, h0)) return kDiscard;
+    if (EXACT) {
+      fdiv = recip_div_ok(p, d, bc.w);
+      inv = make_float3(d.x == 0.0f ? 0.0f : 1.0f / d.x, d.y == 0.0f ? 0.0f : 1.0f / d.y,
+                        d.z == 0.0f ? 0.0f : 1.0f / d.z);
+    } else {
+      e0 = h0;
+    }
     e = h0;
     return kRunning;
   }
@@ -107,7 +123,10 @@ struct Walker {
   // Cube and entry point of level lv replayed from the root along the path.
   __device__ __forceinline__ void replay_to(const Stack& st, int lv, float4 bc, float4& c, float4& en) const {
     c = bc;
-    en = e0;
+    if (EXACT)
+      entry(bc, en);  // the ray was entered, so this succeeds
+    else
+      en = e0;
     for (int k = 0; k < lv; ++k) {
       uint32_t pk = slot(st, k, 0);
       int cc = list_entry(pk, list_next(pk) - 1);
@@ -137,9 +156,16 @@ struct Walker {
     float3 hl = hlf_of(cube);
     // a ray parallel to a bisecting plane has no hit on it (the shader's
     // FLT_MAX sentinel fails the face test)
-    float4 hz = hit_zplane_raw(hl.z, p, d);
-    float4 hx = hit_xplane_raw(hl.x, p, d);
-    float4 hy = hit_yplane_raw(hl.y, p, d);
+    float4 hz, hx, hy;
+    if (EXACT && __all_sync(__activemask(), fdiv)) {
+      hz = hit_zplane_rcp(hl.z, p, d, inv.z);
+      hx = hit_xplane_rcp(hl.x, p, d, inv.x);
+      hy = hit_yplane_rcp(hl.y, p, d, inv.y);
+    } else {
+      hz = hit_zplane_raw(hl.z, p, d);
+      hx = hit_xplane_raw(hl.x, p, d);
+      hy = hit_yplane_raw(hl.y, p, d);
+    }
     bool vz = (d.z != 0.0f) & (hz.w > 0.0f) & in_zface(hz, cube, cb);
     bool vx = (d.x != 0.0f) & (hx.w > 0.0f) & in_xface(hx, cube, cb);
     bool vy = (d.y != 0.0f) & (hy.w > 0.0f) & in_yface(hy, cube, cb);
@@ -275,7 +301,12 @@ struct Walker {
         cube = rc;
         isp = re;
       }
-      if (src != 0) isp = plane_point(src, cube, p, d);
+      if (src != 0) {
+        if (EXACT && __all_sync(__activemask(), fdiv))
+          isp = plane_point_rcp(src, cube, p, d, inv);
+        else
+          isp = plane_point(src, cube, p, d);
+      }
       int32_t ps = (int32_t)slot(st, level, 1);
       cs = load_child(sc.tree[0], ps, level, cc & 7, oob);
       if (DYN) {
