@@ -339,7 +339,7 @@ int qbc_load_flat(qbc_ctx* ctx, int tree, const char* pnt_path, const char* col_
  * (device outputs, these render options) on the context's stream under
  * candidate tuning options, one option after another with the others kept
  * at their best so far: the service threshold (1..16), the warp tile width
- * (4, 8, 16, 32) and the render blocks per SM (0, 2..8). Each candidate gets
+ * (2, 4, 8, 16, 32) and the render blocks per SM (0, 2..8). Each candidate gets
  * one untimed frame, then `reps` (1..101) frames timed with CUDA events; its
  * time is their median. The fastest setting stays set on the context (the
  * initial one on error). The options change only the time of a frame, never
@@ -443,7 +443,7 @@ int qbc_synchronize(qbc_ctx* ctx);
  *   is at least this (0: always).
  *   QBC_OPT_PROPOSAL_COUNT  1..3, default 3: network proposals tried per
  *   pixel, earliest first.
- *   QBC_OPT_TILE_WIDTH  4, 8 (default), 16 or 32: width of the 32-pixel warp
+ *   QBC_OPT_TILE_WIDTH  2, 4, 8 (default), 16 or 32: width of the 32-pixel warp
  *   tiles the render kernels take from their queue (height 32 / width).
  *   QBC_OPT_BLOCKS_PER_SM  0 (default: as many as fit) .. 32: resident
  *   render blocks per SM of the persistent grid.

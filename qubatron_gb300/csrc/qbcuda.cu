@@ -244,9 +244,9 @@ extern "C" int qbc_set_option(qbc_ctx* c, int option, int value) {
     return QBC_OK;
   }
   if (option == QBC_OPT_TILE_WIDTH) {
-    if (value != 4 && value != 8 && value != 16 && value != 32)
-      return fail(QBC_E_ARG, "qbc_set_option: tile width %d (4, 8, 16 or 32)", value);
-    c->tile_shift = value == 4 ? 2 : value == 8 ? 3 : value == 16 ? 4 : 5;
+    if (value != 2 && value != 4 && value != 8 && value != 16 && value != 32)
+      return fail(QBC_E_ARG, "qbc_set_option: tile width %d (2, 4, 8, 16 or 32)", value);
+    c->tile_shift = value == 2 ? 1 : value == 4 ? 2 : value == 8 ? 3 : value == 16 ? 4 : 5;
     return QBC_OK;
   }
   if (option == QBC_OPT_BLOCKS_PER_SM) {
@@ -1429,7 +1429,7 @@ int autotune_impl(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs, in
   // one option at a time, each kept at its best before the next is swept
   for (int sm : {1, 2, 3, 4, 6, 8, 12, 16})
     if (sm != best->service && (rc = consider({best->shift, best->blocks, sm}))) return rc;
-  for (int sh : {2, 3, 4, 5})
+  for (int sh : {1, 2, 3, 4, 5})
     if (sh != best->shift && (rc = consider({sh, best->blocks, best->service}))) return rc;
   for (int bl : {0, 2, 3, 4, 6, 8})
     if (bl != best->blocks && (rc = consider({best->shift, bl, best->service}))) return rc;

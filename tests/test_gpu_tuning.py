@@ -50,7 +50,7 @@ def test_options_do_not_change_pixels(ctx, floor50k_scene, two_pass):
     upload_scene(ctx, s.nodes, s.colors, s.normals)
     views = _views()
     ref = _render(ctx, views, two_pass)
-    for tw in (4, 16, 32, 8):
+    for tw in (2, 4, 16, 32, 8):
         ctx.set_option(L.OPT_TILE_WIDTH, tw)
         for bl in (2, 0):
             ctx.set_option(L.OPT_BLOCKS_PER_SM, bl)
@@ -74,14 +74,15 @@ def test_autotune(ctx, floor50k_scene):
         o.rgba8 = f.data_ptr()
         outs.append(o)
     r = ctx.autotune(views, outs, reps=3)
-    assert r["tile_width"] in (4, 8, 16, 32) and r["blocks_per_sm"] in (0, 2, 3, 4, 6, 8)
-    assert 1 <= r["service_min"] <= 16 and r["candidates"] >= 15
+    assert r["tile_width"] in (2, 4, 8, 16, 32) and r["blocks_per_sm"] in (0, 2, 3, 4, 6, 8)
+    assert 1 <= r["service_min"] <= 16 and r["candidates"] >= 16
     assert 0 < r["ms_best"] <= r["ms_initial"]
     assert ctx.get_option(L.OPT_TILE_WIDTH) == r["tile_width"]
     assert ctx.get_option(L.OPT_BLOCKS_PER_SM) == r["blocks_per_sm"]
     assert ctx.get_option(L.OPT_SERVICE_MIN) == r["service_min"]
     _same(ref, ctx.render_host(views, ALL), "after autotune")
-    for opt, bad in ((L.OPT_TILE_WIDTH, 6), (L.OPT_TILE_WIDTH, 64), (L.OPT_BLOCKS_PER_SM, 33), (L.OPT_SERVICE_MIN, 0)):
+    for opt, bad in ((L.OPT_TILE_WIDTH, 6), (L.OPT_TILE_WIDTH, 1), (L.OPT_TILE_WIDTH, 64), (L.OPT_BLOCKS_PER_SM, 33),
+                     (L.OPT_SERVICE_MIN, 0)):
         with pytest.raises(QbcError):
             ctx.set_option(opt, bad)
     with pytest.raises(QbcError):
