@@ -1,0 +1,323 @@
+// Frame graphs (qbc_graph_*) and the autotuner (qbc_autotune) of libqbcuda:
+// both drive whole frames through render_views_impl on a context's stream.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "qbc_ctx.h"
+
+// ---------------------------------------------------------------------------
+// A frame as a CUDA graph
+// ---------------------------------------------------------------------------
+
+namespace {
+
+// Everything a captured frame bakes into its kernel parameters besides the
+// views: device addresses and sizes of the trees, models and work buffers,
+// and the options that become launch parameters.
+struct FrameSignature {
+  qbc::DevScene scene;
+  const void* rec;
+  int64_t rec_cap;
+  const void* pixlog;
+  int64_t pixlog_cap;
+  const void* net_w;
+  const void* net_b;
+  const void* stream;
+  int32_t service_min;
+  int32_t proposal_gate;
+  int32_t tile_shift;
+  int32_t blocks_per_sm;
+  int32_t proposal_count;
+};
+
+bool same_signature(const FrameSignature& a, const FrameSignature& b) {
+  for (int t = 0; t < 2; ++t) {
+    const qbc::DevTree &ta = a.scene.tree[t], &tb = b.scene.tree[t];
+    const qbc::DevModel &ma = a.scene.model[t], &mb = b.scene.model[t];
+    if (ta.child != tb.child || ta.model != tb.model || ta.n != tb.n) return false;
+    if (ma.col != mb.col || ma.nrm != mb.nrm || ma.n != mb.n) return false;
+  }
+  return a.rec == b.rec && a.rec_cap == b.rec_cap && a.pixlog == b.pixlog && a.pixlog_cap == b.pixlog_cap &&
+         a.net_w == b.net_w && a.net_b == b.net_b && a.stream == b.stream && a.service_min == b.service_min &&
+         a.proposal_gate == b.proposal_gate && a.tile_shift == b.tile_shift && a.blocks_per_sm == b.blocks_per_sm &&
+         a.proposal_count == b.proposal_count;
+}
+
+FrameSignature frame_signature(const qbc_ctx* c) {
+  FrameSignature f;
+  f.scene = device_scene(c);
+  f.rec = c->rec;
+  f.rec_cap = c->rec_cap;
+  f.pixlog = c->pixlog;
+  f.pixlog_cap = c->pixlog_cap;
+  f.net_w = c->net.wb;
+  f.net_b = c->net.master;
+  f.stream = c->stream;
+  f.service_min = c->service_min;
+  f.proposal_gate = c->proposal_gate;
+  f.tile_shift = c->tile_shift;
+  f.blocks_per_sm = c->blocks_per_sm;
+  f.proposal_count = c->proposal_count;
+  return f;
+}
+
+
+}  // namespace
+
+struct qbc_graph {
+  qbc_ctx* ctx = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<qbc_outputs> outs;
+  std::vector<int32_t> sizes;  // width, height per view
+  qbc_render_opts opts;
+  bool has_opts = false;
+  int n = 0;
+  int64_t kernels = 0;
+  FrameSignature sig;
+};
+
+namespace {
+
+int capture_frame(qbc_graph* g, const qbc_view* views, cudaGraph_t* out) {
+  qbc_ctx* c = g->ctx;
+  QBC_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  const int rc = render_views_impl(c, views, g->outs.data(), g->n, 1, g->has_opts ? &g->opts : nullptr, nullptr);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+  if (rc || e != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+    return rc ? rc : cuda_fail(e, "frame capture");
+  }
+  *out = graph;
+  return QBC_OK;
+}
+
+int64_t kernel_nodes(cudaGraph_t graph) {
+  size_t n = 0;
+  if (cudaGraphGetNodes(graph, nullptr, &n) != cudaSuccess) return 0;
+  std::vector<cudaGraphNode_t> nodes(n);
+  if (n && cudaGraphGetNodes(graph, nodes.data(), &n) != cudaSuccess) return 0;
+  int64_t k = 0;
+  for (cudaGraphNode_t node : nodes) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(node, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+  }
+  return k;
+}
+
+void release_graph(qbc_graph* g) {
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  g->exec = nullptr;
+  g->graph = nullptr;
+}
+
+}  // namespace
+
+// The context is going: free the graph's CUDA objects; the handle stays
+// valid for qbc_graph_destroy and fails every other call.
+void detach_graph(qbc_graph* g) {
+  release_graph(g);
+  g->ctx = nullptr;
+}
+
+extern "C" int qbc_graph_capture(qbc_ctx* c, const qbc_view* views, const qbc_outputs* dev_outs, int n,
+                                 const qbc_render_opts* opts, qbc_graph** out) {
+  qbc::clear_error();
+  if (!c || !views || !dev_outs || !out || n <= 0) return fail(QBC_E_ARG, "qbc_graph_capture: bad argument");
+  int rc = check_render_opts(opts, n);
+  if (rc) return rc;
+  QBC_CUDA(cudaSetDevice(c->device));
+  // one eager frame first: buffers grown and kernel attributes set before
+  // the capture, which must not allocate
+  rc = render_views_impl(c, views, dev_outs, n, 1, opts, nullptr);
+  if (rc) return rc;
+  QBC_CUDA(cudaStreamSynchronize(c->stream));
+  std::unique_ptr<qbc_graph> g(new qbc_graph());
+  g->ctx = c;
+  g->n = n;
+  g->outs.assign(dev_outs, dev_outs + n);
+  for (int i = 0; i < n; ++i) {
+    g->sizes.push_back(views[i].width_px);
+    g->sizes.push_back(views[i].height_px);
+  }
+  std::memset(&g->opts, 0, sizeof(g->opts));
+  if (opts) {
+    g->opts = *opts;
+    g->has_opts = true;
+  }
+  g->sig = frame_signature(c);
+  rc = capture_frame(g.get(), views, &g->graph);
+  if (rc) return rc;
+  cudaError_t e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+  if (e != cudaSuccess) {
+    release_graph(g.get());
+    return cuda_fail(e, "qbc_graph_capture: instantiate");
+  }
+  g->kernels = kernel_nodes(g->graph);
+  c->graphs.push_back(g.get());
+  *out = g.release();
+  return QBC_OK;
+}
+
+extern "C" int qbc_graph_update(qbc_graph* g, const qbc_view* views, int n) {
+  qbc::clear_error();
+  if (!g || !views || n != g->n) return fail(QBC_E_ARG, "qbc_graph_update: bad argument (views must match the capture)");
+  if (!g->ctx) return fail(QBC_E_STATE, "qbc_graph_update: the graph's context was destroyed");
+  for (int i = 0; i < n; ++i)
+    if (views[i].width_px != g->sizes[2 * i] || views[i].height_px != g->sizes[2 * i + 1])
+      return fail(QBC_E_ARG, "qbc_graph_update: view %d is %dx%d, captured %dx%d", i, views[i].width_px,
+                  views[i].height_px, g->sizes[2 * i], g->sizes[2 * i + 1]);
+  qbc_ctx* c = g->ctx;
+  QBC_CUDA(cudaSetDevice(c->device));
+  g->sig = frame_signature(c);
+  cudaGraph_t fresh = nullptr;
+  int rc = capture_frame(g, views, &fresh);
+  if (rc) return rc;
+  cudaGraphExecUpdateResultInfo info;
+  if (cudaGraphExecUpdate(g->exec, fresh, &info) != cudaSuccess) {
+    // a different topology (e.g. another kernel variant): instantiate anew
+    cudaGetLastError();
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t e = cudaGraphInstantiate(&exec, fresh, 0);
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(fresh);
+      return cuda_fail(e, "qbc_graph_update: instantiate");
+    }
+    cudaGraphExecDestroy(g->exec);
+    g->exec = exec;
+  }
+  cudaGraphDestroy(g->graph);
+  g->graph = fresh;
+  g->kernels = kernel_nodes(fresh);
+  return QBC_OK;
+}
+
+extern "C" int qbc_graph_launch(qbc_graph* g) {
+  qbc::clear_error();
+  if (!g) return fail(QBC_E_ARG, "qbc_graph_launch: null graph");
+  if (!g->ctx || !g->exec) return fail(QBC_E_STATE, "qbc_graph_launch: the graph's context was destroyed");
+  qbc_ctx* c = g->ctx;
+  if (!same_signature(frame_signature(c), g->sig))
+    return fail(QBC_E_STATE, "qbc_graph_launch: scene, buffers, stream or options changed since the capture "
+                             "(qbc_graph_update re-captures)");
+  QBC_CUDA(cudaSetDevice(c->device));
+  QBC_CUDA(cudaGraphLaunch(g->exec, c->stream));
+  c->launches += g->kernels;
+  return QBC_OK;
+}
+
+extern "C" int qbc_graph_destroy(qbc_graph* g) {
+  if (!g) return QBC_OK;
+  if (qbc_ctx* c = g->ctx) {
+    cudaSetDevice(c->device);
+    c->graphs.erase(std::remove(c->graphs.begin(), c->graphs.end(), g), c->graphs.end());
+  }
+  release_graph(g);
+  delete g;
+  return QBC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner: service threshold, warp tile width, render blocks per SM
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct TuneSetting {
+  int shift, blocks, service;
+};
+
+// Median device time of `reps` frames (after one untimed frame).
+int time_frames(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs, int n, const qbc_render_opts* opts,
+                int reps, cudaEvent_t* ev, float* ms) {
+  int rc = render_views_impl(c, views, outs, n, 1, opts, nullptr);
+  if (rc) return rc;
+  std::vector<float> t((size_t)reps);
+  for (int r = 0; r < reps; ++r) {
+    QBC_CUDA(cudaEventRecord(ev[0], c->stream));
+    rc = render_views_impl(c, views, outs, n, 1, opts, nullptr);
+    if (rc) return rc;
+    QBC_CUDA(cudaEventRecord(ev[1], c->stream));
+    QBC_CUDA(cudaEventSynchronize(ev[1]));
+    QBC_CUDA(cudaEventElapsedTime(&t[(size_t)r], ev[0], ev[1]));
+  }
+  std::sort(t.begin(), t.end());
+  *ms = t[(size_t)reps / 2];
+  return QBC_OK;
+}
+
+int autotune_impl(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs, int n, const qbc_render_opts* opts,
+                  int reps, cudaEvent_t* ev, TuneSetting* best, qbc_tune_result* res) {
+  auto apply = [c](const TuneSetting& s) {
+    c->tile_shift = s.shift;
+    c->blocks_per_sm = s.blocks;
+    c->service_min = s.service;
+  };
+  float best_ms = 0.0f;
+  int rc = time_frames(c, views, outs, n, opts, reps, ev, &best_ms);
+  if (rc) return rc;
+  res->ms_initial = best_ms;
+  res->candidates = 1;
+  auto consider = [&](const TuneSetting& s) -> int {
+    apply(s);
+    float ms = 0.0f;
+    int e = time_frames(c, views, outs, n, opts, reps, ev, &ms);
+    if (e) return e;
+    ++res->candidates;
+    if (ms < best_ms) {
+      best_ms = ms;
+      *best = s;
+    }
+    return QBC_OK;
+  };
+  // one option at a time, each kept at its best before the next is swept
+  for (int sm : {1, 2, 3, 4, 6, 8, 12, 16})
+    if (sm != best->service && (rc = consider({best->shift, best->blocks, sm}))) return rc;
+  for (int sh : {1, 2, 3, 4, 5})
+    if (sh != best->shift && (rc = consider({sh, best->blocks, best->service}))) return rc;
+  for (int bl : {0, 2, 3, 4, 6, 8})
+    if (bl != best->blocks && (rc = consider({best->shift, bl, best->service}))) return rc;
+  res->ms_best = best_ms;
+  return QBC_OK;
+}
+
+}  // namespace
+
+extern "C" int qbc_autotune(qbc_ctx* c, const qbc_view* views, const qbc_outputs* dev_outs, int n,
+                            const qbc_render_opts* opts, int reps, qbc_tune_result* result) {
+  qbc::clear_error();
+  if (!c || !views || !dev_outs || !result || n <= 0) return fail(QBC_E_ARG, "qbc_autotune: bad argument");
+  if (reps < 1 || reps > 101) return fail(QBC_E_ARG, "qbc_autotune: reps %d outside 1..101", reps);
+  int rc = check_render_opts(opts, n);
+  if (rc) return rc;
+  QBC_CUDA(cudaSetDevice(c->device));
+  std::memset(result, 0, sizeof(*result));
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  QBC_CUDA(cudaEventCreate(&ev[0]));
+  if (cudaEventCreate(&ev[1]) != cudaSuccess) {
+    cudaEventDestroy(ev[0]);
+    return fail(QBC_E_CUDA, "qbc_autotune: event");
+  }
+  const TuneSetting initial{c->tile_shift, c->blocks_per_sm, c->service_min};
+  TuneSetting best = initial;
+  rc = autotune_impl(c, views, dev_outs, n, opts, reps, ev, &best, result);
+  const TuneSetting keep = rc ? initial : best;
+  c->tile_shift = keep.shift;
+  c->blocks_per_sm = keep.blocks;
+  c->service_min = keep.service;
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  if (rc) return rc;
+  result->tile_width = 1 << keep.shift;
+  result->blocks_per_sm = keep.blocks;
+  result->service_min = keep.service;
+  return QBC_OK;
+}

@@ -1,4 +1,6 @@
-// libqbcuda: context, uploads and the render kernel behind include/qbcuda.h.
+// libqbcuda: context, uploads, tree builds and edits, and the render kernels
+// behind include/qbcuda.h (frame graphs and the autotuner are in frame.cu,
+// the occluder network in proposal.cu).
 //
 // The kernels are in render.cuh (per-pixel shader body, persistent) and
 // walker.cuh (the traversal). Build flags: -fmad=false -prec-div=true
@@ -14,13 +16,7 @@
 #include <new>
 #include <vector>
 
-#include "qbc_internal.h"
-#include "qbcuda.h"
-#include "mlp.h"
-#include "mlp_device.cuh"
-#include "render.cuh"
-
-using qbc::fail;
+#include "qbc_ctx.h"
 
 namespace qbc {
 
@@ -46,120 +42,6 @@ __global__ void expand_attr_kernel(const float* __restrict__ raw, int64_t n, flo
 // ---------------------------------------------------------------------------
 // Context
 // ---------------------------------------------------------------------------
-
-struct DevTreeBuf {
-  int4* child = nullptr;
-  int32_t* model = nullptr;
-  int64_t n = 0;    // node count of the array last uploaded
-  int64_t cap = 0;  // nodes allocated
-};
-
-struct DevModelBuf {
-  float4* col = nullptr;
-  float4* nrm = nullptr;
-  int64_t n_col = 0, n_nrm = 0;
-  int64_t cap_col = 0, cap_nrm = 0;
-};
-
-struct qbc_ctx {
-  int device = 0;
-  int sm_count = 0;
-  cudaStream_t own = nullptr;
-  cudaStream_t stream = nullptr;
-  DevTreeBuf tree[2];
-  DevModelBuf model[2];
-  void* stage = nullptr;  // device staging for uploads
-  size_t stage_bytes = 0;
-  void* scratch = nullptr;  // device outputs for host-output renders
-  size_t scratch_bytes = 0;
-  unsigned int* queue = nullptr;  // global tile counter of the persistent render kernel
-  // two-pass render: records, counters (queued, shade-pass next), statistics, per-pixel log
-  uint32_t* rec = nullptr;
-  int64_t rec_cap = 0;
-  unsigned int* wcount = nullptr;
-  unsigned long long* wstats = nullptr;
-  float* pixlog = nullptr;
-  int64_t pixlog_cap = 0;
-  int64_t pixlog_valid = 0;  // pixels of the last logged render (0: none)
-  // occluder-proposal network and its training set
-  qbc::mlp::Net net;
-  __nv_bfloat16* ds_x = nullptr;  // features, kIn per sample
-  float* ds_t = nullptr;          // first-occluder t
-  int8_t* ds_kind = nullptr;      // 1 occluded, 0 lit
-  int64_t ds_cap = 0;
-  unsigned int* ds_count = nullptr;
-  bool fused_attr[2] = {false, false};  // dynamic shared memory set for the fused network kernels
-  std::vector<qbc_graph*> graphs;       // captured frames, detached when the context goes
-  int render_blocks[4] = {0, 0, 0, 0};  // resident blocks per SM of each render_kernel variant
-  int attr_done = 0;
-  int service_min = qbc::kServiceMinDefault;
-  int tile_shift = 3;     // 8x4 warp tiles
-  int blocks_per_sm = 0;  // render blocks per SM (0: as many as fit)
-  int proposal_gate = 500;  // per mille: minimum predicted occlusion probability to try a proposal
-  int proposal_count = 3;   // network proposals tried per pixel (earliest first)
-  int64_t launches = 0;
-};
-
-namespace {
-
-constexpr size_t kStageMax = size_t(256) << 20;
-
-int cuda_fail(cudaError_t e, const char* what) {
-  return fail(QBC_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
-}
-
-#define QBC_CUDA(call)                            \
-  do {                                            \
-    cudaError_t e_ = (call);                      \
-    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
-  } while (0)
-
-int ensure_stage(qbc_ctx* c, size_t bytes) {
-  if (c->stage_bytes >= bytes) return QBC_OK;
-  if (c->stage) QBC_CUDA(cudaFree(c->stage));
-  c->stage = nullptr;
-  c->stage_bytes = 0;
-  cudaError_t e = cudaMalloc(&c->stage, bytes);
-  if (e != cudaSuccess) return fail(QBC_E_NOMEM, "staging buffer of %zu bytes: %s", bytes, cudaGetErrorString(e));
-  c->stage_bytes = bytes;
-  return QBC_OK;
-}
-
-template <typename T>
-int grow(T** p, int64_t* cap, int64_t need, size_t elem_bytes, const char* what) {
-  if (*cap >= need) return QBC_OK;
-  if (*p) QBC_CUDA(cudaFree(*p));
-  *p = nullptr;
-  *cap = 0;
-  cudaError_t e = cudaMalloc((void**)p, (size_t)need * elem_bytes);
-  if (e != cudaSuccess)
-    return fail(QBC_E_NOMEM, "%s: %lld items: %s", what, (long long)need, cudaGetErrorString(e));
-  *cap = need;
-  return QBC_OK;
-}
-
-int launch_grid(const qbc_ctx* c, int64_t n) {
-  int64_t blocks = (n + 255) / 256;
-  int64_t maxb = (int64_t)std::max(c->sm_count, 1) * 16;
-  return (int)std::max<int64_t>(1, std::min(blocks, maxb));
-}
-
-qbc::DevScene device_scene(const qbc_ctx* c) {
-  qbc::DevScene s;
-  for (int t = 0; t < 2; ++t) {
-    s.tree[t].child = c->tree[t].child;
-    s.tree[t].model = c->tree[t].model;
-    s.tree[t].n = (int32_t)c->tree[t].n;
-    s.model[t].col = c->model[t].col;
-    s.model[t].nrm = c->model[t].nrm;
-    // the colour and normal arrays are separate uploads; a point index is
-    // valid when both hold it
-    s.model[t].n = (int32_t)std::min(c->model[t].n_col, c->model[t].n_nrm);
-  }
-  return s;
-}
-
-}  // namespace
 
 extern "C" int qbc_create(int device, qbc_ctx** out) {
   qbc::clear_error();
@@ -189,8 +71,6 @@ extern "C" int qbc_create(int device, qbc_ctx** out) {
   *out = c;
   return QBC_OK;
 }
-
-void detach_graph(qbc_graph* g);
 
 extern "C" int qbc_destroy(qbc_ctx* c) {
   if (!c) return QBC_OK;
@@ -682,230 +562,45 @@ extern "C" int qbc_download_tree(qbc_ctx* c, int tree, int32_t* nodes, int64_t c
 }
 
 // ---------------------------------------------------------------------------
-// Occluder-proposal network: features, dataset, training, inference
-// ---------------------------------------------------------------------------
-
-namespace {
-
-using bf16 = __nv_bfloat16;
-
-// Network input of a shade-pass record: hit point normalised to the
-// basecube, unit normal, unit direction to the light, and sin/cos of pi
-// times the normalised hit point scaled by 4, 8, ..., 128 (45 values, zero
-// padded).
-__device__ __forceinline__ void record_features(const qbc::Batch& b, const uint32_t* r, bf16* x) {
-  const qbc_view& v = b.job[r[qbc::kPxView]].v;
-  const float S = v.basecube[3];
-  const float lo[3] = {v.basecube[0], v.basecube[1] - S, v.basecube[2] - S};
-  float f[qbc::mlp::kIn];
-  float isp[3], n[3], l[3];
-  for (int k = 0; k < 3; ++k) {
-    isp[k] = __uint_as_float(r[qbc::kPxIsp + k]);
-    n[k] = __uint_as_float(r[qbc::kPxNrm + k]);
-    l[k] = v.light[k] - isp[k];
-  }
-  const float nn = rsqrtf(fmaxf(n[0] * n[0] + n[1] * n[1] + n[2] * n[2], 1e-20f));
-  const float ll = rsqrtf(fmaxf(l[0] * l[0] + l[1] * l[1] + l[2] * l[2], 1e-20f));
-  for (int k = 0; k < 3; ++k) {
-    f[k] = (isp[k] - lo[k]) / S;
-    f[3 + k] = n[k] * nn;
-    f[6 + k] = l[k] * ll;
-  }
-  int o = 9;
-  for (int q = 0; q < 6; ++q) {
-    const float sc = (float)(4 << q);
-    for (int k = 0; k < 3; ++k) {
-      f[o++] = sinpif(sc * f[k]);
-      f[o++] = cospif(sc * f[k]);
-    }
-  }
-  for (; o < qbc::mlp::kIn; ++o) f[o] = 0.0f;
-  for (int k = 0; k < qbc::mlp::kIn; ++k) x[k] = __float2bfloat16(f[k]);
-}
-
-// Shaded records of a logged render -> training samples (appended).
-__global__ void collect_kernel(const __grid_constant__ qbc::Batch b, const __grid_constant__ qbc::Wave w,
-                               bf16* __restrict__ X, float* __restrict__ tl, int8_t* __restrict__ kind,
-                               unsigned int* __restrict__ count, int64_t cap) {
-  const unsigned total = min(*w.qcount, w.cap);
-  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
-    const uint32_t* r = w.rec + (size_t)q * qbc::kRecWords;
-    if (!(r[qbc::kPxFlags] & QBC_PX_SHADED)) continue;
-    const float t = __uint_as_float(r[qbc::kRecLogT]);
-    const bool lit = r[qbc::kRecLogLit] != 0;
-    const bool occluded = !lit && t > 0.0f && t < 1.0f;
-    if (!lit && !occluded) continue;  // unlit without an occluder before the hit: no label
-    const unsigned i = atomicAdd(count, 1u);
-    if ((int64_t)i >= cap) continue;
-    record_features(b, r, X + (size_t)i * qbc::mlp::kIn);
-    tl[i] = occluded ? t : 2.0f;
-    kind[i] = occluded ? 1 : 0;
-  }
-}
-
-// Fused-network rows over the shade-pass record queue: the features of each
-// record in, its proposals out (earliest first; none where the occlusion
-// logit is below the gate). The row count is read on the device.
-struct RecordRows {
-  qbc::Batch b;
-  qbc::Wave w;
-  float gate;
-  int keep;  // proposals kept, earliest first
-  __device__ __forceinline__ uint32_t rows() const { return min(*w.qcount, w.cap); }
-  __device__ __forceinline__ void load(uint32_t r0, uint32_t n, bf16* x, int lane) const {
-    if (lane >= 16) return;
-    bf16* row = x + lane * qbc::mlp::kLdIn;
-    if ((uint32_t)lane < n) {
-      record_features(b, w.rec + (size_t)(r0 + lane) * qbc::kRecWords, row);
-    } else {
-      for (int k = 0; k < qbc::mlp::kIn; ++k) row[k] = __float2bfloat16(0.0f);
-    }
-  }
-  __device__ __forceinline__ void store(uint32_t r, const float* o) const {
-    float t[3] = {o[0], o[1], o[2]};
-    if (!(o[qbc::mlp::kGate] >= gate)) t[0] = t[1] = t[2] = -1.0f;
-    for (int i = 0; i < 2; ++i)
-      for (int j = i + 1; j < 3; ++j)
-        if (t[j] < t[i]) {
-          const float x = t[i];
-          t[i] = t[j];
-          t[j] = x;
-        }
-    for (int k = keep; k < 3; ++k) t[k] = -1.0f;
-    uint32_t* rec = w.rec + (size_t)r * qbc::kRecWords;
-    for (int k = 0; k < 3; ++k) rec[qbc::kRecProp + k] = __float_as_uint(t[k]);
-  }
-};
-
-// Fused-network rows over a bf16 feature matrix (kIn per row) -> kOutUsed
-// floats per row.
-struct MatrixRows {
-  const bf16* X;
-  float* out;
-  uint32_t m;
-  __device__ __forceinline__ uint32_t rows() const { return m; }
-  __device__ __forceinline__ void load(uint32_t r0, uint32_t n, bf16* x, int lane) const {
-    constexpr int kVec = qbc::mlp::kIn / 8;
-    for (int e = lane; e < 16 * kVec; e += 32) {
-      const int r = e / kVec, c = e % kVec;
-      uint4 v = make_uint4(0u, 0u, 0u, 0u);
-      if ((uint32_t)r < n) v = reinterpret_cast<const uint4*>(X + (size_t)(r0 + r) * qbc::mlp::kIn)[c];
-      *reinterpret_cast<uint4*>(x + r * qbc::mlp::kLdIn + c * 8) = v;
-    }
-  }
-  __device__ __forceinline__ void store(uint32_t r, const float* o) const {
-    for (int k = 0; k < qbc::mlp::kOutUsed; ++k) out[(size_t)r * qbc::mlp::kOutUsed + k] = o[k];
-  }
-};
-
-// Random minibatch of the training set.
-__global__ void gather_kernel(const bf16* __restrict__ X, const float* __restrict__ tl,
-                              const int8_t* __restrict__ kind, int64_t n, int64_t rows, uint64_t seed,
-                              bf16* __restrict__ bx, float* __restrict__ bt, int8_t* __restrict__ bk) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < rows; i += (int64_t)gridDim.x * blockDim.x) {
-    uint64_t z = seed + 0x9E3779B97F4A7C15ull * (uint64_t)(i + 1);
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    z ^= z >> 31;
-    const int64_t j = (int64_t)(z % (uint64_t)n);
-    for (int k = 0; k < qbc::mlp::kIn; ++k) bx[i * qbc::mlp::kIn + k] = X[j * qbc::mlp::kIn + k];
-    bt[i] = tl[j];
-    bk[i] = kind[j];
-  }
-}
-
-bf16 host_bf16(float f) {
-  // round to nearest even (NaN kept quiet)
-  uint32_t u;
-  std::memcpy(&u, &f, 4);
-  if ((u & 0x7fffffffu) > 0x7f800000u) return __ushort_as_bfloat16((unsigned short)((u >> 16) | 0x40));
-  u += 0x7fffu + ((u >> 16) & 1u);
-  return __ushort_as_bfloat16((unsigned short)(u >> 16));
-}
-
-// One launch of the fused network over `src`'s rows: a persistent grid of
-// resident blocks, each staging the weights once.
-template <class Src>
-int launch_fused(qbc_ctx* c, const Src& src, int variant) {
-  using qbc::mlp::FusedSmem;
-  auto kern = qbc::mlp::fused_forward_kernel<Src>;
-  if (!c->fused_attr[variant]) {
-    QBC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FusedSmem)));
-    c->fused_attr[variant] = true;
-  }
-  int per_sm = 0;
-  QBC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, qbc::mlp::kFusedThreads, sizeof(FusedSmem)));
-  if (per_sm < 1) return fail(QBC_E_STATE, "proposal network: no block fits on an SM");
-  qbc::mlp::FusedParams p;
-  for (int l = 0; l < 4; ++l) {
-    p.w[l] = c->net.wb + qbc::mlp::param_offset(l, false);
-    p.b[l] = c->net.master + qbc::mlp::param_offset(l, true);
-    if (reinterpret_cast<uintptr_t>(p.w[l]) % 16) return fail(QBC_E_STATE, "proposal network: unaligned weights");
-  }
-  kern<<<per_sm * c->sm_count, qbc::mlp::kFusedThreads, sizeof(FusedSmem), c->stream>>>(p, src);
-  QBC_CUDA(cudaGetLastError());
-  ++c->launches;
-  return QBC_OK;
-}
-
-// Proposals of every queued record from the network (no host round trip:
-// the kernel reads the queue length on the device).
-int propose_mlp(qbc_ctx* c, const qbc::Batch& b, const qbc::Wave& w) {
-  if (!c->net.ready) return fail(QBC_E_STATE, "qbc_render_views_ex: no occluder network in this context");
-  std::unique_ptr<RecordRows> src(new RecordRows());
-  src->b = b;
-  src->w = w;
-  const float p = (float)c->proposal_gate * 1e-3f;  // gate probability -> logit
-  src->gate = c->proposal_gate <= 0 ? -INFINITY : logf(p / (1.0f - p));
-  src->keep = c->proposal_count;
-  return launch_fused(c, *src, 0);
-}
-
-int ensure_dataset(qbc_ctx* c, int64_t cap) {
-  if (c->ds_cap >= cap) return QBC_OK;
-  // grow keeping the samples collected so far
-  bf16* x = nullptr;
-  float* t = nullptr;
-  int8_t* k = nullptr;
-  cudaError_t e = cudaMalloc(&x, (size_t)cap * qbc::mlp::kIn * 2);
-  if (e == cudaSuccess) e = cudaMalloc(&t, (size_t)cap * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&k, (size_t)cap);
-  if (e == cudaSuccess && !c->ds_count) e = cudaMalloc(&c->ds_count, sizeof(unsigned));
-  if (e != cudaSuccess) {
-    cudaFree(x);
-    cudaFree(t);
-    cudaFree(k);
-    return fail(QBC_E_NOMEM, "proposal training set of %lld samples: %s", (long long)cap, cudaGetErrorString(e));
-  }
-  unsigned have = 0;
-  if (c->ds_cap > 0) {
-    QBC_CUDA(cudaMemcpyAsync(&have, c->ds_count, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
-    QBC_CUDA(cudaStreamSynchronize(c->stream));
-    have = (unsigned)std::min<int64_t>(have, c->ds_cap);
-    QBC_CUDA(cudaMemcpyAsync(x, c->ds_x, (size_t)have * qbc::mlp::kIn * 2, cudaMemcpyDeviceToDevice, c->stream));
-    QBC_CUDA(cudaMemcpyAsync(t, c->ds_t, (size_t)have * 4, cudaMemcpyDeviceToDevice, c->stream));
-    QBC_CUDA(cudaMemcpyAsync(k, c->ds_kind, (size_t)have, cudaMemcpyDeviceToDevice, c->stream));
-    QBC_CUDA(cudaStreamSynchronize(c->stream));
-  }
-  cudaFree(c->ds_x);
-  cudaFree(c->ds_t);
-  cudaFree(c->ds_kind);
-  c->ds_x = x;
-  c->ds_t = t;
-  c->ds_kind = k;
-  c->ds_cap = cap;
-  QBC_CUDA(cudaMemcpyAsync(c->ds_count, &have, sizeof(unsigned), cudaMemcpyHostToDevice, c->stream));
-  QBC_CUDA(cudaStreamSynchronize(c->stream));
-  return QBC_OK;
-}
-
-}  // namespace
-
-// ---------------------------------------------------------------------------
 // Render
 // ---------------------------------------------------------------------------
 
-namespace {
+namespace qbc {
+
+// Proposals for the records of a two-pass render: the t of the first leaf a
+// previous plain walk of the same pixel logged (when it shadowed), or seeded
+// pseudo-random t values (exactness tests exercise the proposal path with
+// both).
+__global__ void fill_logged_proposals(const __grid_constant__ Batch batch, const __grid_constant__ Wave wave) {
+  const unsigned total = min(*wave.qcount, wave.cap);
+  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+    uint32_t* r = wave.rec + (size_t)q * kRecWords;
+    const ViewJob& J = batch.job[r[kPxView]];
+    const uint32_t xy = r[kPxXY];
+    const float t = wave.pixlog[J.pixel_begin + (int64_t)(xy >> 16) * J.v.width_px + (xy & 0xFFFFu)];
+    reinterpret_cast<float&>(r[kRecProp]) = t;
+    reinterpret_cast<float&>(r[kRecProp + 1]) = -1.0f;
+    reinterpret_cast<float&>(r[kRecProp + 2]) = -1.0f;
+  }
+}
+
+__global__ void fill_random_proposals(const __grid_constant__ Wave wave, unsigned long long seed) {
+  const unsigned total = min(*wave.qcount, wave.cap);
+  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+    uint32_t* r = wave.rec + (size_t)q * kRecWords;
+    unsigned long long z = seed + 0x9E3779B97F4A7C15ull * (r[kPxXY] + 0x10001ull * r[kPxView] + 1);
+    for (int k = 0; k < 3; ++k) {
+      z += 0x9E3779B97F4A7C15ull;
+      unsigned long long x = z;
+      x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+      x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+      x ^= x >> 31;
+      reinterpret_cast<float&>(r[kRecProp + k]) = (float)(x >> 40) * (1.0f / 16777216.0f);
+    }
+  }
+}
+
+}  // namespace qbc
 
 int check_view(const qbc_view& v, int i) {
   if (v.width_px < 1 || v.height_px < 1 || v.width_px > 65536 || v.height_px > 65536)
@@ -914,6 +609,8 @@ int check_view(const qbc_view& v, int i) {
     return fail(QBC_E_ARG, "view %d: maxlevel %d outside 0..%d", i, v.maxlevel, QBC_MAX_LEVEL);
   return QBC_OK;
 }
+
+namespace {
 
 // Bytes per pixel of each output stream, in qbc_outputs order.
 constexpr size_t kOutBytes[6] = {4, 16, 4, 16, 16, 16};
@@ -929,7 +626,6 @@ void** out_slot(qbc_outputs& o, int k) {
   }
 }
 
-int propose_mlp(qbc_ctx* c, const qbc::Batch& b, const qbc::Wave& w);
 
 // Statistics of the shade passes of the last two-pass render (synchronizes).
 int read_stats(qbc_ctx* c, qbc_render_stats* stats) {
@@ -1060,11 +756,18 @@ int launch_batch(qbc_ctx* c, const qbc_view* views, const qbc_outputs* dev_outs,
 
 }  // namespace
 
-namespace {
-int render_views_impl(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs, int n, int outputs_on_device,
-                      const qbc_render_opts* opts, qbc_render_stats* stats);
-int check_render_opts(const qbc_render_opts* opts, int n);
+int check_render_opts(const qbc_render_opts* opts, int n) {
+  if (opts && (opts->proposals < QBC_PROPOSE_NONE || opts->proposals > QBC_PROPOSE_RANDOM))
+    return fail(QBC_E_ARG, "qbc_render_views_ex: unknown proposal source %d", opts->proposals);
+  if (opts && opts->proposals != QBC_PROPOSE_NONE && !opts->two_pass)
+    return fail(QBC_E_ARG, "qbc_render_views_ex: proposals need two_pass");
+  if (opts && (opts->proposal_level < 0 || opts->proposal_level > QBC_MAX_LEVEL))
+    return fail(QBC_E_ARG, "qbc_render_views_ex: proposal_level %d outside 0..%d", opts->proposal_level, QBC_MAX_LEVEL);
+  if (opts && opts->two_pass && n > qbc::kMaxViewsPerLaunch)
+    return fail(QBC_E_ARG, "qbc_render_views_ex: two-pass renders take at most %d views per call", qbc::kMaxViewsPerLaunch);
+  return QBC_OK;
 }
+
 
 extern "C" int qbc_render_views(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs, int n,
                                 int outputs_on_device) {
@@ -1080,7 +783,6 @@ extern "C" int qbc_render_views_ex(qbc_ctx* c, const qbc_view* views, const qbc_
   return render_views_impl(c, views, outs, n, outputs_on_device, opts, stats);
 }
 
-namespace {
 int render_views_impl(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs, int n, int outputs_on_device,
                       const qbc_render_opts* opts, qbc_render_stats* stats) {
   if (!c || (n > 0 && (!views || !outs))) return fail(QBC_E_ARG, "qbc_render_views: null argument");
@@ -1144,330 +846,6 @@ int render_views_impl(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs
   }
   QBC_CUDA(cudaStreamSynchronize(c->stream));
   return two ? read_stats(c, stats) : QBC_OK;
-}
-}  // namespace
-
-// ---------------------------------------------------------------------------
-// A frame as a CUDA graph
-// ---------------------------------------------------------------------------
-
-namespace {
-
-// Everything a captured frame bakes into its kernel parameters besides the
-// views: device addresses and sizes of the trees, models and work buffers,
-// and the options that become launch parameters.
-struct FrameSignature {
-  qbc::DevScene scene;
-  const void* rec;
-  int64_t rec_cap;
-  const void* pixlog;
-  int64_t pixlog_cap;
-  const void* net_w;
-  const void* net_b;
-  const void* stream;
-  int32_t service_min;
-  int32_t proposal_gate;
-  int32_t tile_shift;
-  int32_t blocks_per_sm;
-  int32_t proposal_count;
-};
-
-bool same_signature(const FrameSignature& a, const FrameSignature& b) {
-  for (int t = 0; t < 2; ++t) {
-    const qbc::DevTree &ta = a.scene.tree[t], &tb = b.scene.tree[t];
-    const qbc::DevModel &ma = a.scene.model[t], &mb = b.scene.model[t];
-    if (ta.child != tb.child || ta.model != tb.model || ta.n != tb.n) return false;
-    if (ma.col != mb.col || ma.nrm != mb.nrm || ma.n != mb.n) return false;
-  }
-  return a.rec == b.rec && a.rec_cap == b.rec_cap && a.pixlog == b.pixlog && a.pixlog_cap == b.pixlog_cap &&
-         a.net_w == b.net_w && a.net_b == b.net_b && a.stream == b.stream && a.service_min == b.service_min &&
-         a.proposal_gate == b.proposal_gate && a.tile_shift == b.tile_shift && a.blocks_per_sm == b.blocks_per_sm &&
-         a.proposal_count == b.proposal_count;
-}
-
-FrameSignature frame_signature(const qbc_ctx* c) {
-  FrameSignature f;
-  f.scene = device_scene(c);
-  f.rec = c->rec;
-  f.rec_cap = c->rec_cap;
-  f.pixlog = c->pixlog;
-  f.pixlog_cap = c->pixlog_cap;
-  f.net_w = c->net.wb;
-  f.net_b = c->net.master;
-  f.stream = c->stream;
-  f.service_min = c->service_min;
-  f.proposal_gate = c->proposal_gate;
-  f.tile_shift = c->tile_shift;
-  f.blocks_per_sm = c->blocks_per_sm;
-  f.proposal_count = c->proposal_count;
-  return f;
-}
-
-int check_render_opts(const qbc_render_opts* opts, int n) {
-  if (opts && (opts->proposals < QBC_PROPOSE_NONE || opts->proposals > QBC_PROPOSE_RANDOM))
-    return fail(QBC_E_ARG, "qbc_render_views_ex: unknown proposal source %d", opts->proposals);
-  if (opts && opts->proposals != QBC_PROPOSE_NONE && !opts->two_pass)
-    return fail(QBC_E_ARG, "qbc_render_views_ex: proposals need two_pass");
-  if (opts && (opts->proposal_level < 0 || opts->proposal_level > QBC_MAX_LEVEL))
-    return fail(QBC_E_ARG, "qbc_render_views_ex: proposal_level %d outside 0..%d", opts->proposal_level, QBC_MAX_LEVEL);
-  if (opts && opts->two_pass && n > qbc::kMaxViewsPerLaunch)
-    return fail(QBC_E_ARG, "qbc_render_views_ex: two-pass renders take at most %d views per call", qbc::kMaxViewsPerLaunch);
-  return QBC_OK;
-}
-
-}  // namespace
-
-struct qbc_graph {
-  qbc_ctx* ctx = nullptr;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  std::vector<qbc_outputs> outs;
-  std::vector<int32_t> sizes;  // width, height per view
-  qbc_render_opts opts;
-  bool has_opts = false;
-  int n = 0;
-  int64_t kernels = 0;
-  FrameSignature sig;
-};
-
-namespace {
-
-int capture_frame(qbc_graph* g, const qbc_view* views, cudaGraph_t* out) {
-  qbc_ctx* c = g->ctx;
-  QBC_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-  const int rc = render_views_impl(c, views, g->outs.data(), g->n, 1, g->has_opts ? &g->opts : nullptr, nullptr);
-  cudaGraph_t graph = nullptr;
-  const cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
-  if (rc || e != cudaSuccess) {
-    if (graph) cudaGraphDestroy(graph);
-    cudaGetLastError();
-    return rc ? rc : cuda_fail(e, "frame capture");
-  }
-  *out = graph;
-  return QBC_OK;
-}
-
-int64_t kernel_nodes(cudaGraph_t graph) {
-  size_t n = 0;
-  if (cudaGraphGetNodes(graph, nullptr, &n) != cudaSuccess) return 0;
-  std::vector<cudaGraphNode_t> nodes(n);
-  if (n && cudaGraphGetNodes(graph, nodes.data(), &n) != cudaSuccess) return 0;
-  int64_t k = 0;
-  for (cudaGraphNode_t node : nodes) {
-    cudaGraphNodeType t;
-    if (cudaGraphNodeGetType(node, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
-  }
-  return k;
-}
-
-void release_graph(qbc_graph* g) {
-  if (g->exec) cudaGraphExecDestroy(g->exec);
-  if (g->graph) cudaGraphDestroy(g->graph);
-  g->exec = nullptr;
-  g->graph = nullptr;
-}
-
-}  // namespace
-
-// The context is going: free the graph's CUDA objects; the handle stays
-// valid for qbc_graph_destroy and fails every other call.
-void detach_graph(qbc_graph* g) {
-  release_graph(g);
-  g->ctx = nullptr;
-}
-
-extern "C" int qbc_graph_capture(qbc_ctx* c, const qbc_view* views, const qbc_outputs* dev_outs, int n,
-                                 const qbc_render_opts* opts, qbc_graph** out) {
-  qbc::clear_error();
-  if (!c || !views || !dev_outs || !out || n <= 0) return fail(QBC_E_ARG, "qbc_graph_capture: bad argument");
-  int rc = check_render_opts(opts, n);
-  if (rc) return rc;
-  QBC_CUDA(cudaSetDevice(c->device));
-  // one eager frame first: buffers grown and kernel attributes set before
-  // the capture, which must not allocate
-  rc = render_views_impl(c, views, dev_outs, n, 1, opts, nullptr);
-  if (rc) return rc;
-  QBC_CUDA(cudaStreamSynchronize(c->stream));
-  std::unique_ptr<qbc_graph> g(new qbc_graph());
-  g->ctx = c;
-  g->n = n;
-  g->outs.assign(dev_outs, dev_outs + n);
-  for (int i = 0; i < n; ++i) {
-    g->sizes.push_back(views[i].width_px);
-    g->sizes.push_back(views[i].height_px);
-  }
-  std::memset(&g->opts, 0, sizeof(g->opts));
-  if (opts) {
-    g->opts = *opts;
-    g->has_opts = true;
-  }
-  g->sig = frame_signature(c);
-  rc = capture_frame(g.get(), views, &g->graph);
-  if (rc) return rc;
-  cudaError_t e = cudaGraphInstantiate(&g->exec, g->graph, 0);
-  if (e != cudaSuccess) {
-    release_graph(g.get());
-    return cuda_fail(e, "qbc_graph_capture: instantiate");
-  }
-  g->kernels = kernel_nodes(g->graph);
-  c->graphs.push_back(g.get());
-  *out = g.release();
-  return QBC_OK;
-}
-
-extern "C" int qbc_graph_update(qbc_graph* g, const qbc_view* views, int n) {
-  qbc::clear_error();
-  if (!g || !views || n != g->n) return fail(QBC_E_ARG, "qbc_graph_update: bad argument (views must match the capture)");
-  if (!g->ctx) return fail(QBC_E_STATE, "qbc_graph_update: the graph's context was destroyed");
-  for (int i = 0; i < n; ++i)
-    if (views[i].width_px != g->sizes[2 * i] || views[i].height_px != g->sizes[2 * i + 1])
-      return fail(QBC_E_ARG, "qbc_graph_update: view %d is %dx%d, captured %dx%d", i, views[i].width_px,
-                  views[i].height_px, g->sizes[2 * i], g->sizes[2 * i + 1]);
-  qbc_ctx* c = g->ctx;
-  QBC_CUDA(cudaSetDevice(c->device));
-  g->sig = frame_signature(c);
-  cudaGraph_t fresh = nullptr;
-  int rc = capture_frame(g, views, &fresh);
-  if (rc) return rc;
-  cudaGraphExecUpdateResultInfo info;
-  if (cudaGraphExecUpdate(g->exec, fresh, &info) != cudaSuccess) {
-    // a different topology (e.g. another kernel variant): instantiate anew
-    cudaGetLastError();
-    cudaGraphExec_t exec = nullptr;
-    cudaError_t e = cudaGraphInstantiate(&exec, fresh, 0);
-    if (e != cudaSuccess) {
-      cudaGraphDestroy(fresh);
-      return cuda_fail(e, "qbc_graph_update: instantiate");
-    }
-    cudaGraphExecDestroy(g->exec);
-    g->exec = exec;
-  }
-  cudaGraphDestroy(g->graph);
-  g->graph = fresh;
-  g->kernels = kernel_nodes(fresh);
-  return QBC_OK;
-}
-
-extern "C" int qbc_graph_launch(qbc_graph* g) {
-  qbc::clear_error();
-  if (!g) return fail(QBC_E_ARG, "qbc_graph_launch: null graph");
-  if (!g->ctx || !g->exec) return fail(QBC_E_STATE, "qbc_graph_launch: the graph's context was destroyed");
-  qbc_ctx* c = g->ctx;
-  if (!same_signature(frame_signature(c), g->sig))
-    return fail(QBC_E_STATE, "qbc_graph_launch: scene, buffers, stream or options changed since the capture "
-                             "(qbc_graph_update re-captures)");
-  QBC_CUDA(cudaSetDevice(c->device));
-  QBC_CUDA(cudaGraphLaunch(g->exec, c->stream));
-  c->launches += g->kernels;
-  return QBC_OK;
-}
-
-extern "C" int qbc_graph_destroy(qbc_graph* g) {
-  if (!g) return QBC_OK;
-  if (qbc_ctx* c = g->ctx) {
-    cudaSetDevice(c->device);
-    c->graphs.erase(std::remove(c->graphs.begin(), c->graphs.end(), g), c->graphs.end());
-  }
-  release_graph(g);
-  delete g;
-  return QBC_OK;
-}
-
-// ---------------------------------------------------------------------------
-// Autotuner: service threshold, warp tile width, render blocks per SM
-// ---------------------------------------------------------------------------
-
-namespace {
-
-struct TuneSetting {
-  int shift, blocks, service;
-};
-
-// Median device time of `reps` frames (after one untimed frame).
-int time_frames(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs, int n, const qbc_render_opts* opts,
-                int reps, cudaEvent_t* ev, float* ms) {
-  int rc = render_views_impl(c, views, outs, n, 1, opts, nullptr);
-  if (rc) return rc;
-  std::vector<float> t((size_t)reps);
-  for (int r = 0; r < reps; ++r) {
-    QBC_CUDA(cudaEventRecord(ev[0], c->stream));
-    rc = render_views_impl(c, views, outs, n, 1, opts, nullptr);
-    if (rc) return rc;
-    QBC_CUDA(cudaEventRecord(ev[1], c->stream));
-    QBC_CUDA(cudaEventSynchronize(ev[1]));
-    QBC_CUDA(cudaEventElapsedTime(&t[(size_t)r], ev[0], ev[1]));
-  }
-  std::sort(t.begin(), t.end());
-  *ms = t[(size_t)reps / 2];
-  return QBC_OK;
-}
-
-int autotune_impl(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs, int n, const qbc_render_opts* opts,
-                  int reps, cudaEvent_t* ev, TuneSetting* best, qbc_tune_result* res) {
-  auto apply = [c](const TuneSetting& s) {
-    c->tile_shift = s.shift;
-    c->blocks_per_sm = s.blocks;
-    c->service_min = s.service;
-  };
-  float best_ms = 0.0f;
-  int rc = time_frames(c, views, outs, n, opts, reps, ev, &best_ms);
-  if (rc) return rc;
-  res->ms_initial = best_ms;
-  res->candidates = 1;
-  auto consider = [&](const TuneSetting& s) -> int {
-    apply(s);
-    float ms = 0.0f;
-    int e = time_frames(c, views, outs, n, opts, reps, ev, &ms);
-    if (e) return e;
-    ++res->candidates;
-    if (ms < best_ms) {
-      best_ms = ms;
-      *best = s;
-    }
-    return QBC_OK;
-  };
-  // one option at a time, each kept at its best before the next is swept
-  for (int sm : {1, 2, 3, 4, 6, 8, 12, 16})
-    if (sm != best->service && (rc = consider({best->shift, best->blocks, sm}))) return rc;
-  for (int sh : {1, 2, 3, 4, 5})
-    if (sh != best->shift && (rc = consider({sh, best->blocks, best->service}))) return rc;
-  for (int bl : {0, 2, 3, 4, 6, 8})
-    if (bl != best->blocks && (rc = consider({best->shift, bl, best->service}))) return rc;
-  res->ms_best = best_ms;
-  return QBC_OK;
-}
-
-}  // namespace
-
-extern "C" int qbc_autotune(qbc_ctx* c, const qbc_view* views, const qbc_outputs* dev_outs, int n,
-                            const qbc_render_opts* opts, int reps, qbc_tune_result* result) {
-  qbc::clear_error();
-  if (!c || !views || !dev_outs || !result || n <= 0) return fail(QBC_E_ARG, "qbc_autotune: bad argument");
-  if (reps < 1 || reps > 101) return fail(QBC_E_ARG, "qbc_autotune: reps %d outside 1..101", reps);
-  int rc = check_render_opts(opts, n);
-  if (rc) return rc;
-  QBC_CUDA(cudaSetDevice(c->device));
-  std::memset(result, 0, sizeof(*result));
-  cudaEvent_t ev[2] = {nullptr, nullptr};
-  QBC_CUDA(cudaEventCreate(&ev[0]));
-  if (cudaEventCreate(&ev[1]) != cudaSuccess) {
-    cudaEventDestroy(ev[0]);
-    return fail(QBC_E_CUDA, "qbc_autotune: event");
-  }
-  const TuneSetting initial{c->tile_shift, c->blocks_per_sm, c->service_min};
-  TuneSetting best = initial;
-  rc = autotune_impl(c, views, dev_outs, n, opts, reps, ev, &best, result);
-  const TuneSetting keep = rc ? initial : best;
-  c->tile_shift = keep.shift;
-  c->blocks_per_sm = keep.blocks;
-  c->service_min = keep.service;
-  cudaEventDestroy(ev[0]);
-  cudaEventDestroy(ev[1]);
-  if (rc) return rc;
-  result->tile_width = 1 << keep.shift;
-  result->blocks_per_sm = keep.blocks;
-  result->service_min = keep.service;
-  return QBC_OK;
 }
 
 extern "C" int qbc_trace_rays(qbc_ctx* c, const float* pos, const float* dir, int64_t n, const float basecube[4],
@@ -1668,240 +1046,6 @@ extern "C" int qbc_render_views_noalloc(qbc_ctx* c, const qbc_view* views, const
     if (rc) return rc;
   }
   return QBC_OK;
-}
-
-// ---------------------------------------------------------------------------
-// Occluder-proposal network: C ABI
-// ---------------------------------------------------------------------------
-
-namespace {
-// Host rows of 45 floats -> device bf16 rows of 48.
-int upload_features(qbc_ctx* c, const float* x, int64_t m, bf16** out) {
-  std::vector<bf16> h((size_t)m * qbc::mlp::kIn);
-  for (int64_t i = 0; i < m; ++i)
-    for (int k = 0; k < qbc::mlp::kIn; ++k)
-      h[(size_t)i * qbc::mlp::kIn + k] = host_bf16(k < qbc::mlp::kInUsed ? x[i * qbc::mlp::kInUsed + k] : 0.0f);
-  cudaError_t e = cudaMalloc(out, h.size() * 2);
-  if (e != cudaSuccess) return fail(QBC_E_NOMEM, "proposal features: %s", cudaGetErrorString(e));
-  QBC_CUDA(cudaMemcpyAsync(*out, h.data(), h.size() * 2, cudaMemcpyHostToDevice, c->stream));
-  return QBC_OK;
-}
-}  // namespace
-
-static_assert(QBC_PROPOSAL_PARAMS == 41360, "parameter count");
-
-extern "C" int qbc_proposal_collect(qbc_ctx* c, const qbc_view* views, int n, int64_t* samples) {
-  qbc::clear_error();
-  if (!c || n < 0 || (n > 0 && !views)) return fail(QBC_E_ARG, "qbc_proposal_collect: bad argument");
-  if (n > qbc::kMaxViewsPerLaunch)
-    return fail(QBC_E_ARG, "qbc_proposal_collect: at most %d views per call", qbc::kMaxViewsPerLaunch);
-  QBC_CUDA(cudaSetDevice(c->device));
-  int64_t pixels = 0;
-  for (int i = 0; i < n; ++i) {
-    int rc = check_view(views[i], i);
-    if (rc) return rc;
-    pixels += (int64_t)views[i].width_px * views[i].height_px;
-  }
-  int rc = ensure_dataset(c, std::max<int64_t>(c->ds_cap, c->ds_cap == 0 ? pixels : 0));
-  if (rc) return rc;
-  if (n > 0) {
-    std::vector<qbc_outputs> none(n);
-    std::memset(none.data(), 0, sizeof(qbc_outputs) * n);
-    qbc_render_opts o;
-    std::memset(&o, 0, sizeof(o));
-    o.two_pass = 1;
-    o.log = 1;
-    rc = render_views_impl(c, views, none.data(), n, 1, &o, nullptr);
-    if (rc) return rc;
-    // room for every shaded pixel of this batch
-    unsigned have = 0, queued = 0;
-    QBC_CUDA(cudaMemcpyAsync(&have, c->ds_count, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
-    QBC_CUDA(cudaMemcpyAsync(&queued, c->wcount, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
-    QBC_CUDA(cudaStreamSynchronize(c->stream));
-    rc = ensure_dataset(c, std::max<int64_t>(c->ds_cap, (int64_t)have + queued));
-    if (rc) return rc;
-    // rebuild the batch parameters of that render for the feature kernel
-    qbc::Batch* b = new qbc::Batch();
-    for (int i = 0; i < n; ++i) b->job[i].v = views[i];
-    b->n = n;
-    qbc::Wave w{};
-    w.rec = c->rec;
-    w.qcount = c->wcount;
-    w.cap = (uint32_t)std::min<int64_t>(c->rec_cap, 0xFFFFFFFFll);
-    collect_kernel<<<launch_grid(c, queued), 256, 0, c->stream>>>(*b, w, c->ds_x, c->ds_t, c->ds_kind,
-                                                                  c->ds_count, c->ds_cap);
-    delete b;
-    QBC_CUDA(cudaGetLastError());
-    ++c->launches;
-  }
-  unsigned cnt = 0;
-  if (c->ds_count) {
-    QBC_CUDA(cudaMemcpyAsync(&cnt, c->ds_count, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
-    QBC_CUDA(cudaStreamSynchronize(c->stream));
-  }
-  if (samples) *samples = std::min<int64_t>(cnt, c->ds_cap);
-  return QBC_OK;
-}
-
-extern "C" int qbc_proposal_train(qbc_ctx* c, const qbc_train_opts* opts, qbc_train_stats* stats) {
-  qbc::clear_error();
-  if (!c || !opts) return fail(QBC_E_ARG, "qbc_proposal_train: null argument");
-  if (opts->steps < 0 || opts->batch < 64 || opts->batch > (1 << 22) || !(opts->lr > 0.0f))
-    return fail(QBC_E_ARG, "qbc_proposal_train: steps >= 0, batch 64..4M and lr > 0 required");
-  QBC_CUDA(cudaSetDevice(c->device));
-  unsigned cnt = 0;
-  if (c->ds_count) {
-    QBC_CUDA(cudaMemcpyAsync(&cnt, c->ds_count, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
-    QBC_CUDA(cudaStreamSynchronize(c->stream));
-  }
-  const int64_t n = std::min<int64_t>(cnt, c->ds_cap);
-  if (n == 0) return fail(QBC_E_STATE, "qbc_proposal_train: empty training set (qbc_proposal_collect first)");
-  if (!c->net.ready) {
-    int rc = c->net.init(opts->seed, c->stream);
-    if (rc) return rc;
-  }
-  const int64_t B = opts->batch;
-  bf16* bx = nullptr;
-  float* bt = nullptr;
-  int8_t* bk = nullptr;
-  float* dloss = nullptr;
-  cudaError_t e = cudaMalloc(&bx, (size_t)B * qbc::mlp::kIn * 2);
-  if (e == cudaSuccess) e = cudaMalloc(&bt, (size_t)B * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&bk, (size_t)B);
-  if (e == cudaSuccess) e = cudaMalloc(&dloss, 4);
-  int rc = QBC_OK;
-  if (e != cudaSuccess) rc = fail(QBC_E_NOMEM, "qbc_proposal_train: %s", cudaGetErrorString(e));
-  float first = 0.0f, last = 0.0f;
-  int nlast = 0;
-  for (int step = 0; step < opts->steps && rc == QBC_OK; ++step) {
-    gather_kernel<<<launch_grid(c, B), 256, 0, c->stream>>>(c->ds_x, c->ds_t, c->ds_kind, n, B,
-                                                            opts->seed * 1000003ull + (uint64_t)step, bx, bt, bk);
-    const int64_t l0 = qbc::mlp::launches();
-    rc = c->net.gradient(bx, bt, bk, B, dloss, c->stream);
-    if (rc) break;
-    rc = c->net.adam(opts->lr, c->stream);
-    if (rc) break;
-    c->launches += 1 + (qbc::mlp::launches() - l0);
-    if (step == 0 || step >= opts->steps - 10) {
-      float l = 0.0f;
-      e = cudaMemcpyAsync(&l, dloss, 4, cudaMemcpyDeviceToHost, c->stream);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-      if (e != cudaSuccess) {
-        rc = fail(QBC_E_CUDA, "qbc_proposal_train: %s", cudaGetErrorString(e));
-        break;
-      }
-      if (step == 0) first = l;
-      if (step >= opts->steps - 10) {
-        last += l;
-        ++nlast;
-      }
-    }
-  }
-  cudaStreamSynchronize(c->stream);
-  cudaFree(bx);
-  cudaFree(bt);
-  cudaFree(bk);
-  cudaFree(dloss);
-  if (rc) return rc;
-  if (stats) {
-    std::vector<int8_t> k((size_t)n);
-    QBC_CUDA(cudaMemcpy(k.data(), c->ds_kind, (size_t)n, cudaMemcpyDeviceToHost));
-    uint64_t occ = 0;
-    for (int8_t v : k) occ += v == 1;
-    stats->samples = (uint64_t)n;
-    stats->occluded = occ;
-    stats->loss_first = first;
-    stats->loss_last = nlast ? last / nlast : first;
-  }
-  return QBC_OK;
-}
-
-extern "C" int qbc_proposal_clear(qbc_ctx* c) {
-  if (!c) return fail(QBC_E_ARG, "qbc_proposal_clear: null context");
-  if (c->ds_count) {
-    QBC_CUDA(cudaMemsetAsync(c->ds_count, 0, sizeof(unsigned), c->stream));
-    QBC_CUDA(cudaStreamSynchronize(c->stream));
-  }
-  return QBC_OK;
-}
-
-extern "C" int qbc_proposal_get_params(qbc_ctx* c, float* params) {
-  qbc::clear_error();
-  if (!c || !params) return fail(QBC_E_ARG, "qbc_proposal_get_params: null argument");
-  if (!c->net.ready) return fail(QBC_E_STATE, "qbc_proposal_get_params: no network");
-  QBC_CUDA(cudaSetDevice(c->device));
-  return c->net.get(params, c->stream);
-}
-
-extern "C" int qbc_proposal_set_params(qbc_ctx* c, const float* params) {
-  qbc::clear_error();
-  if (!c || !params) return fail(QBC_E_ARG, "qbc_proposal_set_params: null argument");
-  QBC_CUDA(cudaSetDevice(c->device));
-  int rc = c->net.set(params, c->stream);
-  if (rc) return rc;
-  QBC_CUDA(cudaStreamSynchronize(c->stream));
-  return QBC_OK;
-}
-
-extern "C" int qbc_proposal_eval(qbc_ctx* c, const float* x, int64_t m, float* out) {
-  qbc::clear_error();
-  if (!c || (m > 0 && (!x || !out)) || m < 0 || m > (1ll << 31))
-    return fail(QBC_E_ARG, "qbc_proposal_eval: bad argument");
-  if (!c->net.ready) return fail(QBC_E_STATE, "qbc_proposal_eval: no network");
-  if (m == 0) return QBC_OK;
-  QBC_CUDA(cudaSetDevice(c->device));
-  bf16* dx = nullptr;
-  int rc = upload_features(c, x, m, &dx);
-  if (rc) return rc;
-  float* dout = nullptr;
-  cudaError_t e = cudaMalloc(&dout, (size_t)m * qbc::mlp::kOutUsed * 4);
-  if (e != cudaSuccess) {
-    cudaFree(dx);
-    return fail(QBC_E_NOMEM, "qbc_proposal_eval: %s", cudaGetErrorString(e));
-  }
-  MatrixRows src{dx, dout, (uint32_t)m};
-  rc = launch_fused(c, src, 1);
-  if (!rc) {
-    e = cudaMemcpyAsync(out, dout, (size_t)m * qbc::mlp::kOutUsed * 4, cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    if (e != cudaSuccess) rc = fail(QBC_E_CUDA, "qbc_proposal_eval: %s", cudaGetErrorString(e));
-  }
-  cudaFree(dx);
-  cudaFree(dout);
-  return rc;
-}
-
-extern "C" int qbc_proposal_gradient(qbc_ctx* c, const float* x, const float* t, const int8_t* kind, int64_t m,
-                                     float* loss, float* grad) {
-  qbc::clear_error();
-  if (!c || m <= 0 || !x || !t || !kind || !loss || !grad) return fail(QBC_E_ARG, "qbc_proposal_gradient: bad argument");
-  if (!c->net.ready) return fail(QBC_E_STATE, "qbc_proposal_gradient: no network");
-  QBC_CUDA(cudaSetDevice(c->device));
-  bf16* dx = nullptr;
-  int rc = upload_features(c, x, m, &dx);
-  if (rc) return rc;
-  float* dt = nullptr;
-  int8_t* dk = nullptr;
-  float* dl = nullptr;
-  cudaError_t e = cudaMalloc(&dt, (size_t)m * 4);
-  if (e == cudaSuccess) e = cudaMalloc(&dk, (size_t)m);
-  if (e == cudaSuccess) e = cudaMalloc(&dl, 4);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(dt, t, (size_t)m * 4, cudaMemcpyHostToDevice, c->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(dk, kind, (size_t)m, cudaMemcpyHostToDevice, c->stream);
-  if (e != cudaSuccess) rc = fail(QBC_E_CUDA, "qbc_proposal_gradient: %s", cudaGetErrorString(e));
-  if (!rc) rc = c->net.gradient(dx, dt, dk, m, dl, c->stream);
-  if (!rc) {
-    e = cudaMemcpyAsync(loss, dl, 4, cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(grad, c->net.grad, (size_t)QBC_PROPOSAL_PARAMS * 4, cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    if (e != cudaSuccess) rc = fail(QBC_E_CUDA, "qbc_proposal_gradient: %s", cudaGetErrorString(e));
-  }
-  cudaFree(dx);
-  cudaFree(dt);
-  cudaFree(dk);
-  cudaFree(dl);
-  return rc;
 }
 
 extern "C" int qbc_render(qbc_ctx* c, float width, float height, const float position[3], const float angle[3],

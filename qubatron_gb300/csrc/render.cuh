@@ -581,39 +581,6 @@ __global__ void __launch_bounds__(kThreads) render_kernel(DevScene sc, const __g
   }
 }
 
-// Proposals for the records of a two-pass render: the t of the first leaf a
-// previous plain walk of the same pixel logged (when it shadowed), or seeded
-// pseudo-random t values (exactness tests exercise the proposal path with
-// both).
-__global__ void fill_logged_proposals(const __grid_constant__ Batch batch, const __grid_constant__ Wave wave) {
-  const unsigned total = min(*wave.qcount, wave.cap);
-  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
-    uint32_t* r = wave.rec + (size_t)q * kRecWords;
-    const ViewJob& J = batch.job[r[kPxView]];
-    const uint32_t xy = r[kPxXY];
-    const float t = wave.pixlog[J.pixel_begin + (int64_t)(xy >> 16) * J.v.width_px + (xy & 0xFFFFu)];
-    reinterpret_cast<float&>(r[kRecProp]) = t;
-    reinterpret_cast<float&>(r[kRecProp + 1]) = -1.0f;
-    reinterpret_cast<float&>(r[kRecProp + 2]) = -1.0f;
-  }
-}
-
-__global__ void fill_random_proposals(const __grid_constant__ Wave wave, unsigned long long seed) {
-  const unsigned total = min(*wave.qcount, wave.cap);
-  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
-    uint32_t* r = wave.rec + (size_t)q * kRecWords;
-    unsigned long long z = seed + 0x9E3779B97F4A7C15ull * (r[kPxXY] + 0x10001ull * r[kPxView] + 1);
-    for (int k = 0; k < 3; ++k) {
-      z += 0x9E3779B97F4A7C15ull;
-      unsigned long long x = z;
-      x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
-      x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
-      x ^= x >> 31;
-      reinterpret_cast<float&>(r[kRecProp + k]) = (float)(x >> 40) * (1.0f / 16777216.0f);
-    }
-  }
-}
-
 struct RayJob {
   const float* pos;
   const float* dir;

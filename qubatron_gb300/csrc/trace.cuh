@@ -94,16 +94,21 @@ __device__ __forceinline__ float div_by_recip(float a, float b, float y) {
 }
 
 // Whether div_by_recip is exact for every plane hit of a ray from p along d
-// in a cube of edge S (numerators c - p with c a cube coordinate or midpoint
-// in (0, 2S], so |a| is 0 or within [2^-63, 2^66]): quotients and remainders
-// then stay normal. A zero direction component is fine (that plane is never
-// hit).
+// in the basecube (0, S, S, S): numerators c - p with c a cube coordinate
+// (0 or S on the basecube faces) or a midpoint in (0, S) are 0 or within
+// [2^-62, 2^65] in magnitude when every |p| component is 0 or in
+// [2^-62, 2^64] and S in [2^-20, 2^40]; with |d| components 0 or in
+// [2^-40, 2^40] every quotient and remainder then stays normal. A zero
+// direction component is fine (that plane is never hit).
 __device__ __forceinline__ bool recip_div_ok(float3 p, float3 d, float S) {
   auto dir_ok = [](float v) {
     const float a = fabsf(v);
     return (a == 0.0f) | ((a >= 9.094947e-13f) & (a <= 1.0995116e12f));  // 2^-40 .. 2^40
   };
-  auto pos_ok = [](float v) { return fabsf(v) <= 1.8446744e19f; };  // 2^64
+  auto pos_ok = [](float v) {
+    const float a = fabsf(v);
+    return (a == 0.0f) | ((a >= 2.1684043e-19f) & (a <= 1.8446744e19f));  // 2^-62 .. 2^64
+  };
   return dir_ok(d.x) & dir_ok(d.y) & dir_ok(d.z) & pos_ok(p.x) & pos_ok(p.y) & pos_ok(p.z) &
          (S >= 9.536743e-07f) & (S <= 1.0995116e12f);  // 2^-20 .. 2^40
 }

@@ -107,15 +107,14 @@ struct Walker {
     vis_d = 0;
     target = 0;
     tdepth = 0;
-    float4 h0;
-    if (!entry(bc, h0)) return kDiscard;
     if (EXACT) {
       fdiv = recip_div_ok(p, d, bc.w);
-      inv = make_float3(d.x == 0.0f ? 0.0f : 1.0f / d.x, d.y == 0.0f ? 0.0f : 1.0f / d.y,
-                        d.z == 0.0f ? 0.0f : 1.0f / d.z);
-    } else {
-      e0 = h0;
+      inv = make_float3(d.x == 0.0f ? 0.0f : __frcp_rn(d.x), d.y == 0.0f ? 0.0f : __frcp_rn(d.y),
+                        d.z == 0.0f ? 0.0f : __frcp_rn(d.z));
     }
+    float4 h0;
+    if (!entry(bc, h0)) return kDiscard;
+    if (!EXACT) e0 = h0;
     e = h0;
     return kRunning;
   }
