@@ -480,6 +480,7 @@ __global__ void __launch_bounds__(kThreads) render_kernel(DevScene sc, const __g
 #pragma unroll
   for (int k = 0; k < kStatCount; ++k) S.stat[k] = 0;
   int chunk = 0, consumed = 32;  // warp-uniform
+  bool fast = false;             // warp-uniform: see the service phase
   bool exhausted = false;
   const unsigned lt_mask = (1u << lane) - 1u;
   const unsigned total = MODE == kShadePass ? min(*wave.qcount, wave.cap) : (unsigned)batch.tiles_total;
@@ -560,10 +561,13 @@ __global__ void __launch_bounds__(kThreads) render_kernel(DevScene sc, const __g
           }
         }
       }
+      // whether every running lane may divide by its reciprocals (the set
+      // of running rays changes only here)
+      fast = EXACT && __all_sync(0xFFFFFFFFu, !S.running || S.w.fdiv);
       if (exhausted && __ballot_sync(0xFFFFFFFFu, S.phase != kIdle) == 0) break;
     }
     if (S.running) {
-      const int r = S.w.step(sc, S.maxlevel, S.bc, S.st);
+      const int r = S.w.step(sc, S.maxlevel, S.bc, S.st, fast);
       if (r != kRunning) {
         S.running = false;
         S.result = r;
@@ -603,7 +607,7 @@ __global__ void __launch_bounds__(kThreads) rays_kernel(DevScene sc, const __gri
   int r = w.start(job.bc, p, d);
   if (r != kDiscard) {
     do {
-      r = w.step(sc, job.maxlevel, job.bc, st);
+      r = w.step(sc, job.maxlevel, job.bc, st, false);
     } while (r == kRunning);
   }
   int32_t ms = -1, md = -1, ls = -1, ld = -1;

@@ -140,7 +140,9 @@ struct Walker {
   // Every step of every lane thus runs exactly one subnode test, so the
   // lanes of a warp stay on the same instructions for the expensive part.
   // Returns kRunning, kLeaf (fields via leaf()) or kMiss.
-  __device__ __forceinline__ int step(const DevScene& sc, int maxlevel, float4 bc, const Stack& st) {
+  // `fast`: every lane of the warp that steps now may divide by its
+  // reciprocals (a vote the caller takes when rays start).
+  __device__ __forceinline__ int step(const DevScene& sc, int maxlevel, float4 bc, const Stack& st, bool fast) {
     if (level == maxlevel) return kLeaf;
 
     if (EXACT) cube = cube_of_path(bc);
@@ -156,7 +158,7 @@ struct Walker {
     // a ray parallel to a bisecting plane has no hit on it (the shader's
     // FLT_MAX sentinel fails the face test)
     float4 hz, hx, hy;
-    if (EXACT && __all_sync(__activemask(), fdiv)) {
+    if (EXACT && fast) {
       hz = hit_zplane_rcp(hl.z, p, d, inv.z);
       hx = hit_xplane_rcp(hl.x, p, d, inv.x);
       hy = hit_yplane_rcp(hl.y, p, d, inv.y);
@@ -301,7 +303,7 @@ struct Walker {
         isp = re;
       }
       if (src != 0) {
-        if (EXACT && __all_sync(__activemask(), fdiv))
+        if (EXACT && fast)
           isp = plane_point_rcp(src, cube, p, d, inv);
         else
           isp = plane_point(src, cube, p, d);
