@@ -171,9 +171,12 @@ def count_rays(flags: np.ndarray) -> int:
     return primary + shadow + flare
 
 
-def cpu_sample(scene, views, budget_s: float, seed: int = 7, character=None, frame: int = 0):
+def cpu_sample(scene, views, budget_s: float, seed: int = 7, character=None, frame: int = 0, gpu_frames=None):
     """The oracle on a seeded pixel sample of the views, all host cores. With
-    a character, its pose of `frame` is skinned and built on the host."""
+    a character, its pose of `frame` is skinned and built on the host. With
+    gpu_frames (per view: host arrays rgba8, flags, leaf of the same frame
+    rendered on the GPU), every sampled pixel is also compared with it, after
+    the timing."""
     from oracle import qbo
     threads = os.cpu_count() or 1
     if character is not None:
@@ -186,13 +189,17 @@ def cpu_sample(scene, views, budget_s: float, seed: int = 7, character=None, fra
     ov = [qbo.QboView.from_bytes(v.to_bytes()) for v in views]
     rng = np.random.default_rng(seed)
 
+    kept = []  # (view, px, py, oracle outputs) for the parity check
+
     def run(per_view: int):
         rays, t0 = 0, time.perf_counter()
-        for v in ov:
+        for vi, v in enumerate(ov):
             px = rng.integers(0, v.width_px, per_view).astype(np.int32)
             py = rng.integers(0, v.height_px, per_view).astype(np.int32)
             out = qbo.render_pixels(sc, v, px, py, threads)
             rays += count_rays(out["flags"])
+            if gpu_frames is not None:
+                kept.append((vi, px, py, out))
         return rays, time.perf_counter() - t0
 
     # time-boxed: batches of seeded pixels of every view until the budget is spent
@@ -205,10 +212,22 @@ def cpu_sample(scene, views, budget_s: float, seed: int = 7, character=None, fra
         rounds += 1
         if t < budget_s / 8:
             per_view *= 2
-    return {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
-            "sample": f"{rounds} rounds of seeded pixels over all {len(ov)} views of the same workload "
-                      f"({rays} rays, {dt:.1f} s)",
-            "seconds": dt, "rays": rays}
+    res = {"value": rays / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+           "sample": f"{rounds} rounds of seeded pixels over all {len(ov)} views of the same workload "
+                     f"({rays} rays, {dt:.1f} s)",
+           "seconds": dt, "rays": rays}
+    if gpu_frames is not None:
+        # the GPU frame's row is py counted from the bottom (GL order), as the
+        # oracle's pixel coordinates
+        n = bad8 = badf = badl = 0
+        for vi, px, py, out in kept:
+            g = gpu_frames[vi]
+            n += px.size
+            bad8 += int((g["rgba8"][py, px] != out["rgba8"]).any(axis=-1).sum())
+            badf += int((g["flags"][py, px].view(np.uint32) != out["flags"]).sum())
+            badl += int((g["leaf"][py, px] != out["leaf"]).any(axis=-1).sum())
+        res["parity"] = {"pixels": n, "rgba8_mismatch": bad8, "flags_mismatch": badf, "leaf_mismatch": badl}
+    return res
 
 
 def run_reference(args):
@@ -530,9 +549,27 @@ def run_gpu(args):
     if rank == 0 and not args.no_cpu_baseline:
         if scene.nodes is None:
             scene.nodes = ctx.download_tree(False)  # the GPU-built tree, for the host oracle
-        line["cpu_baseline"] = {k: v for k, v in cpu_sample(scene, views, budget_s=args.cpu_seconds,
-                                                            character=character, frame=args.warmup).items()
-                                if k not in ("seconds", "rays")}
+        # the frame the CPU sample renders (the character's pose of frame
+        # `warmup`), once more on the GPU with the streams the check compares
+        update(args.warmup)
+        chk, couts = [], []
+        for v in views:
+            t = {"rgba8": torch.empty((v.height_px, v.width_px, 4), dtype=torch.uint8, device="cuda"),
+                 "flags": torch.empty((v.height_px, v.width_px), dtype=torch.int32, device="cuda"),
+                 "leaf": torch.empty((v.height_px, v.width_px, 4), dtype=torch.int32, device="cuda")}
+            o = qb.Outputs()
+            o.rgba8, o.flags, o.leaf = t["rgba8"].data_ptr(), t["flags"].data_ptr(), t["leaf"].data_ptr()
+            chk.append(t)
+            couts.append(o)
+        ctx.render_views(views, couts, on_device=True)
+        torch.cuda.synchronize()
+        gpu_frames = [{k: a.cpu().numpy() for k, a in t.items()} for t in chk]
+        del chk
+        res = cpu_sample(scene, views, budget_s=args.cpu_seconds, character=character, frame=args.warmup,
+                         gpu_frames=gpu_frames)
+        line["parity_sample"] = res.pop("parity")
+        line["parity_sample"]["streams"] = "rgba8, flags, leaf (GPU frame vs the oracle on the CPU sample's pixels)"
+        line["cpu_baseline"] = {k: v for k, v in res.items() if k not in ("seconds", "rays")}
     ctx.close()
     if rank == 0:
         print(json.dumps(line))
