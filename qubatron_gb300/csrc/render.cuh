@@ -3,7 +3,8 @@
 // render_kernel is the per-pixel body of the reference's fragment shader
 // (src/qubatron/shaders/octree_fsh.c:399-464): ray generation, primary ray,
 // shadow ray from the light, shading, light flare. It is persistent: every
-// warp takes 8x4 pixel tiles from a global queue, and a lane whose ray ended
+// warp takes 32-pixel tiles (8x4 by default, QBC_OPT_TILE_WIDTH) from a
+// global queue, and a lane whose ray ended
 // continues at once with the next ray of its pixel (shadow, flare) or with
 // the next pixel of its warp's tile, so lanes do not idle behind the
 // slowest ray of the warp.

@@ -5,6 +5,7 @@
 // Results are bit-identical to the shader's FP32 arithmetic: this file must be
 // compiled with -fmad=false (no fused multiply-add), IEEE division and sqrt and
 // no flush-to-zero, and every expression keeps the shader's operation order.
+// The only explicit FMAs are those of div_by_recip, an exact division.
 //
 // Stack. The shader keeps per level a cube, four candidate points, four octets
 // and three ints (~1.9 KB per thread, octree_fsh.c:50-58). Here a level keeps
@@ -16,9 +17,9 @@
 //   word 1, 2: the level's node index in the static and dynamic tree.
 // A candidate point is recomputed from its source with the same operations on
 // the same inputs, so it has the same bits as the stored one. The cube of a
-// level is recovered on the way up by undoing the child shift, which is exact
-// when every cube coordinate is representable (checked on the host, EXACT =
-// true), or else by replaying the path from the root.
+// level is computed from the path bits when every cube coordinate is
+// representable (checked on the host, EXACT = true; see walker.cuh), or else
+// replayed from the root along the path.
 #pragma once
 
 #include <cstdint>
@@ -176,17 +177,6 @@ __device__ __forceinline__ float4 child_cube(float4 t, int o) {
   t.w = halfs;
   return t;
 }
-// Inverse of child_cube; exact whenever the forward shift was.
-__device__ __forceinline__ float4 parent_cube(float4 t, int o) {
-  float hs = t.w;
-  float kx = (o & 1) ? 1.0f : 0.0f, ky = (o & 2) ? 1.0f : 0.0f, kz = (o & 4) ? 1.0f : 0.0f;
-  t.x -= kx * hs;
-  t.y += ky * hs;
-  t.z += kz * hs;
-  t.w = hs * 2.0f;
-  return t;
-}
-
 // Point of candidate source src (1 z, 2 x, 3 y bisecting plane) of cube t:
 // hit_{z,x,y}plane of the cube's midpoint, as one plane hit whose axis is
 // picked by selects (the same operations on the same operands, so the same
