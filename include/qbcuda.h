@@ -443,6 +443,11 @@ int qbc_synchronize(qbc_ctx* ctx);
  *   is at least this (0: always).
  *   QBC_OPT_PROPOSAL_COUNT  1..3, default 3: network proposals tried per
  *   pixel, earliest first.
+ *   QBC_OPT_BOX_PRUNE  1 (default) or 0: the walk skips a child whose
+ *   subtree's leaf box (widened by 2^-14 of the basecube edge) the ray
+ *   misses. Pixels never change; only the per-pixel visit counts (the
+ *   `visits` stream) fall below the shader's. 0 walks exactly as the
+ *   shader, visit counts included.
  *   QBC_OPT_TILE_WIDTH  2, 4, 8 (default), 16 or 32: width of the 32-pixel warp
  *   tiles the render kernels take from their queue (height 32 / width).
  *   QBC_OPT_BLOCKS_PER_SM  0 (default: as many as fit) .. 32: resident
@@ -453,6 +458,7 @@ int qbc_synchronize(qbc_ctx* ctx);
 #define QBC_OPT_TILE_WIDTH 3
 #define QBC_OPT_BLOCKS_PER_SM 4
 #define QBC_OPT_PROPOSAL_COUNT 5
+#define QBC_OPT_BOX_PRUNE 6
 int qbc_set_option(qbc_ctx* ctx, int option, int value);
 int qbc_get_option(qbc_ctx* ctx, int option, int* value);
 

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libqbcuda.so")
 
-SOURCES = ["qbcuda.cu", "frame.cu", "proposal.cu", "build.cu", "mlp.cu", "host.cpp"]
+SOURCES = ["qbcuda.cu", "frame.cu", "proposal.cu", "build.cu", "boxes.cu", "mlp.cu", "host.cpp"]
 HEADERS = ["trace.cuh", "walker.cuh", "render.cuh", "qbc_internal.h", "qbc_ctx.h", "mlp.h", "mlp_device.cuh"]
 
 NVCC_FLAGS = [

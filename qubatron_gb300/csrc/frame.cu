@@ -40,6 +40,7 @@ bool same_signature(const FrameSignature& a, const FrameSignature& b) {
     const qbc::DevTree &ta = a.scene.tree[t], &tb = b.scene.tree[t];
     const qbc::DevModel &ma = a.scene.model[t], &mb = b.scene.model[t];
     if (ta.child != tb.child || ta.model != tb.model || ta.n != tb.n) return false;
+    if (ta.cbox != tb.cbox || ta.box_depth != tb.box_depth) return false;
     if (ma.col != mb.col || ma.nrm != mb.nrm || ma.n != mb.n) return false;
   }
   return a.rec == b.rec && a.rec_cap == b.rec_cap && a.pixlog == b.pixlog && a.pixlog_cap == b.pixlog_cap &&
@@ -177,6 +178,9 @@ extern "C" int qbc_graph_update(qbc_graph* g, const qbc_view* views, int n) {
                   views[i].height_px, g->sizes[2 * i], g->sizes[2 * i + 1]);
   qbc_ctx* c = g->ctx;
   QBC_CUDA(cudaSetDevice(c->device));
+  // leaf boxes rebuilt outside the capture (that allocates and synchronises)
+  int brc = ensure_boxes(c);
+  if (brc) return brc;
   g->sig = frame_signature(c);
   cudaGraph_t fresh = nullptr;
   int rc = capture_frame(g, views, &fresh);

@@ -23,6 +23,11 @@ struct DevTreeBuf {
   int32_t* model = nullptr;
   int64_t n = 0;    // node count of the array last uploaded
   int64_t cap = 0;  // nodes allocated
+  // children's leaf boxes for pruning (boxes.cu), rebuilt lazily after a change
+  uint32_t* cbox = nullptr;
+  int64_t cbox_cap = 0;  // nodes
+  int box_depth = -1;
+  bool box_valid = false;
 };
 
 struct DevModelBuf {
@@ -68,6 +73,7 @@ struct qbc_ctx {
   int blocks_per_sm = 0;  // render blocks per SM (0: as many as fit)
   int proposal_gate = 500;  // per mille: minimum predicted occlusion probability to try a proposal
   int proposal_count = 3;   // network proposals tried per pixel (earliest first)
+  int box_prune = 1;        // skip subtrees whose leaf boxes the ray misses
   int64_t launches = 0;
 };
 
@@ -119,6 +125,9 @@ inline qbc::DevScene device_scene(const qbc_ctx* c) {
     s.tree[t].child = c->tree[t].child;
     s.tree[t].model = c->tree[t].model;
     s.tree[t].n = (int32_t)c->tree[t].n;
+    const bool boxes = c->box_prune && c->tree[t].box_valid && c->tree[t].box_depth >= 0;
+    s.tree[t].cbox = boxes ? c->tree[t].cbox : nullptr;
+    s.tree[t].box_depth = boxes ? c->tree[t].box_depth : 0;
     s.model[t].col = c->model[t].col;
     s.model[t].nrm = c->model[t].nrm;
     // the colour and normal arrays are separate uploads; a point index is
@@ -127,6 +136,9 @@ inline qbc::DevScene device_scene(const qbc_ctx* c) {
   }
   return s;
 }
+
+// Rebuild the leaf boxes of trees changed since the last build (allocates).
+int ensure_boxes(qbc_ctx* c);
 
 // Shared entry points of the translation units.
 int check_view(const qbc_view& v, int i);

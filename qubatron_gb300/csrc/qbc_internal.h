@@ -42,4 +42,10 @@ int remove_points(int32_t* child, const int32_t* model, int64_t n_nodes, const f
                   float basesize, int levels, int32_t* d_modind, int32_t* d_octind, int64_t* removed,
                   cudaStream_t stream, int64_t* launches);
 
+// Leaf-box records of every node's children (boxes.cu) for the tree `child`
+// (8 int32 per node, n nodes) into rec (16 words per node); depth gets the
+// tree's depth, or -1 when the array is not a tree the renders can use.
+int build_child_boxes(const int32_t* child, int64_t n, uint32_t* rec, cudaStream_t stream, int* depth,
+                      int64_t* launches);
+
 }  // namespace qbc

@@ -80,6 +80,7 @@ extern "C" int qbc_destroy(qbc_ctx* c) {
   for (int t = 0; t < 2; ++t) {
     cudaFree(c->tree[t].child);
     cudaFree(c->tree[t].model);
+    cudaFree(c->tree[t].cbox);
     cudaFree(c->model[t].col);
     cudaFree(c->model[t].nrm);
   }
@@ -123,6 +124,11 @@ extern "C" int qbc_set_option(qbc_ctx* c, int option, int value) {
     c->proposal_count = value;
     return QBC_OK;
   }
+  if (option == QBC_OPT_BOX_PRUNE) {
+    if (value < 0 || value > 1) return fail(QBC_E_ARG, "qbc_set_option: box pruning %d (0 or 1)", value);
+    c->box_prune = value;
+    return QBC_OK;
+  }
   if (option == QBC_OPT_TILE_WIDTH) {
     if (value != 2 && value != 4 && value != 8 && value != 16 && value != 32)
       return fail(QBC_E_ARG, "qbc_set_option: tile width %d (2, 4, 8, 16 or 32)", value);
@@ -149,6 +155,10 @@ extern "C" int qbc_get_option(qbc_ctx* c, int option, int* value) {
   }
   if (option == QBC_OPT_PROPOSAL_COUNT) {
     *value = c->proposal_count;
+    return QBC_OK;
+  }
+  if (option == QBC_OPT_BOX_PRUNE) {
+    *value = c->box_prune;
     return QBC_OK;
   }
   if (option == QBC_OPT_TILE_WIDTH) {
@@ -242,6 +252,7 @@ int upload_impl(qbc_ctx* c, const void* data, int type, size_t size, size_t item
     }
     hi = std::min(hi, n_total);
     t.n = n_total;
+    t.box_valid = false;  // leaf boxes rebuilt before the next render
     const int64_t chunk = (int64_t)(kStageMax / node_bytes);
     if (hi > lo && !device_src) {
       int rc = ensure_stage(c, (size_t)std::min(hi - lo, chunk) * node_bytes);
@@ -416,6 +427,7 @@ int build_into(qbc_ctx* c, int tree, const float* pnts, const int32_t* octets, i
   c->launches += t.launches;
   if (rc) return rc;
   c->tree[tree].n = t.n_nodes;
+  c->tree[tree].box_valid = false;
   return QBC_OK;
 }
 
@@ -558,6 +570,29 @@ extern "C" int qbc_download_tree(qbc_ctx* c, int tree, int32_t* nodes, int64_t c
     QBC_CUDA(cudaMemcpyAsync(nodes + a * 12, c->stage, (size_t)(b - a) * 48, cudaMemcpyDeviceToHost, c->stream));
   }
   QBC_CUDA(cudaStreamSynchronize(c->stream));
+  return QBC_OK;
+}
+
+int ensure_boxes(qbc_ctx* c) {
+  if (!c->box_prune) return QBC_OK;
+  for (int t = 0; t < 2; ++t) {
+    DevTreeBuf& tb = c->tree[t];
+    if (tb.box_valid) continue;
+    tb.box_depth = -1;
+    if (tb.n > 0) {
+      if (tb.cbox_cap < tb.n) {
+        int rc = grow(&tb.cbox, &tb.cbox_cap, tb.cap > tb.n ? tb.cap : tb.n, 64, "octree leaf boxes");
+        if (rc) return rc;
+      }
+      QBC_CUDA(cudaMemsetAsync(tb.cbox, 0, (size_t)tb.n * 64, c->stream));
+      int depth = -1;
+      int rc = qbc::build_child_boxes(reinterpret_cast<const int32_t*>(tb.child), tb.n, tb.cbox, c->stream, &depth,
+                                      &c->launches);
+      if (rc) return rc;
+      tb.box_depth = depth;
+    }
+    tb.box_valid = true;
+  }
   return QBC_OK;
 }
 
@@ -793,6 +828,8 @@ int render_views_impl(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs
     if (rc) return rc;
   }
 
+  int brc = ensure_boxes(c);
+  if (brc) return brc;
   const bool two = opts && opts->two_pass;
   if (two) QBC_CUDA(cudaMemsetAsync(c->wstats, 0, qbc::kStatCount * sizeof(unsigned long long), c->stream));
   if (outputs_on_device) {
@@ -857,6 +894,10 @@ extern "C" int qbc_trace_rays(qbc_ctx* c, const float* pos, const float* dir, in
     return fail(QBC_E_ARG, "qbc_trace_rays: maxlevel %d outside 0..%d", maxlevel, QBC_MAX_LEVEL);
   if (n == 0) return QBC_OK;
   QBC_CUDA(cudaSetDevice(c->device));
+  {
+    int brc = ensure_boxes(c);
+    if (brc) return brc;
+  }
   qbc_view probe;
   std::memset(&probe, 0, sizeof(probe));
   for (int k = 0; k < 4; ++k) probe.basecube[k] = basecube[k];

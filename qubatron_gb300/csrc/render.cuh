@@ -461,7 +461,7 @@ constexpr int kServiceMinDefault = 4;
 // MODE kShadePass: the queued pixels' shadow rays (first the proposals, with
 // PROP), shading and flare.
 template <bool EXACT, bool DYN, int MODE, bool PROP>
-__global__ void __launch_bounds__(kThreads) render_kernel(DevScene sc, const __grid_constant__ Batch batch,
+__global__ void __launch_bounds__(kThreads, DYN ? 5 : 1) render_kernel(DevScene sc, const __grid_constant__ Batch batch,
                                                           unsigned int* queue, const __grid_constant__ Wave wave) {
   extern __shared__ uint32_t smem[];
   const int tid = threadIdx.x, lane = tid & 31;
@@ -552,7 +552,7 @@ __global__ void __launch_bounds__(kThreads) render_kernel(DevScene sc, const __g
         idle = __ballot_sync(0xFFFFFFFFu, S.phase == kIdle);
       }
       if (go) {
-        if (S.w.start(S.bc, rp, rd) == kDiscard) {
+        if (S.w.start(S.bc, rp, rd, sc, S.maxlevel) == kDiscard) {
           S.discard();
         } else {
           S.running = true;
@@ -564,7 +564,7 @@ __global__ void __launch_bounds__(kThreads) render_kernel(DevScene sc, const __g
       }
       // whether every running lane may divide by its reciprocals (the set
       // of running rays changes only here)
-      fast = EXACT && __all_sync(0xFFFFFFFFu, !S.running || S.w.fdiv);
+      fast = EXACT && __all_sync(0xFFFFFFFFu, !S.running || (S.w.mode & 1u));
       if (exhausted && __ballot_sync(0xFFFFFFFFu, S.phase != kIdle) == 0) break;
     }
     if (S.running) {
@@ -605,7 +605,7 @@ __global__ void __launch_bounds__(kThreads) rays_kernel(DevScene sc, const __gri
   Walker<EXACT, DYN> w;
   float3 p = make_float3(job.pos[3 * i], job.pos[3 * i + 1], job.pos[3 * i + 2]);
   float3 d = make_float3(job.dir[3 * i], job.dir[3 * i + 1], job.dir[3 * i + 2]);
-  int r = w.start(job.bc, p, d);
+  int r = w.start(job.bc, p, d, sc, job.maxlevel);
   if (r != kDiscard) {
     do {
       r = w.step(sc, job.maxlevel, job.bc, st, false);

@@ -36,6 +36,8 @@ struct DevTree {
   const int4* child;     // 2 int4 per node: the 8 child indices
   const int32_t* model;  // slot 8: model index of the point that made the node
   int32_t n;             // nodes held; index >= n reads as 0 and is reported
+  int32_t box_depth;     // depth the leaf boxes were built for (boxes usable when maxlevel >= it)
+  const uint32_t* cbox;  // per node, 16 words: its children's leaf boxes (boxes.cu); null: none
 };
 
 struct DevModel {
@@ -275,5 +277,41 @@ __device__ __forceinline__ int list_len(uint32_t pk) { return (pk >> 20) & 7; }
 __device__ __forceinline__ int list_next(uint32_t pk) { return (pk >> 23) & 7; }
 __device__ __forceinline__ int list_entry(uint32_t pk, int k) { return (pk >> (5 * k)) & 31; }
 
+
+// Whether the ray p + t d (t >= 0) passes within m of the leaf box of child o
+// (its record word r, boxes.cu) of the node whose cube is
+// `cube`. inv = 1 / d with no zero component. A miss proves that the walk
+// finds no leaf below that child: every candidate point it computes lies
+// within a small multiple of the coordinates' ulp of the ray, far below m,
+// and a leaf is only reached through a point inside it.
+__device__ __forceinline__ uint2 child_box_word(const uint32_t* rec, int o) {
+  return __ldg(reinterpret_cast<const uint2*>(rec) + o);
+}
+__device__ __forceinline__ bool child_box_hit(uint2 r, int o, float4 cube, float3 p, float3 inv, float m) {
+  const uint32_t a = r.x, b = r.y;
+  // byte k of w as a float: bits 0x4B0000kk are 2^23 + k
+  auto f8 = [](uint32_t w, uint32_t sel) { return __uint_as_float(__byte_perm(w, 0x4B000000u, sel)) - 8388608.0f; };
+  const float xlo = f8(a, 0x7540u), xhi = f8(a, 0x7541u), ylo = f8(a, 0x7542u), yhi = f8(a, 0x7543u);
+  const float zlo = f8(b, 0x7540u), zhi = f8(b, 0x7541u);
+  const float half = cube.w * 0.5f, unit = half * 0.00390625f;  // 1/256 of the child's edge
+  const float x0 = cube.x + ((o & 1) ? half : 0.0f);
+  const float y0 = cube.y - ((o & 2) ? half : 0.0f);
+  const float z0 = cube.z - ((o & 4) ? half : 0.0f);
+  // world bounds (y and z counted downward from the child's top), widened by m
+  const float bx0 = __fmaf_rn(xlo, unit, x0 - m), bx1 = __fmaf_rn(xhi + 1.0f, unit, x0 + m);
+  const float by0 = __fmaf_rn(-(yhi + 1.0f), unit, y0 - m), by1 = __fmaf_rn(-ylo, unit, y0 + m);
+  const float bz0 = __fmaf_rn(-(zhi + 1.0f), unit, z0 - m), bz1 = __fmaf_rn(-zlo, unit, z0 + m);
+  float t0 = (bx0 - p.x) * inv.x, t1 = (bx1 - p.x) * inv.x;
+  float tn = fminf(t0, t1), tf = fmaxf(t0, t1);
+  t0 = (by0 - p.y) * inv.y;
+  t1 = (by1 - p.y) * inv.y;
+  tn = fmaxf(tn, fminf(t0, t1));
+  tf = fminf(tf, fmaxf(t0, t1));
+  t0 = (bz0 - p.z) * inv.z;
+  t1 = (bz1 - p.z) * inv.z;
+  tn = fmaxf(tn, fminf(t0, t1));
+  tf = fminf(tf, fmaxf(t0, t1));
+  return (xlo <= xhi) & (tn <= tf) & (tf >= 0.0f);  // xlo > xhi: a subtree without leaves
+}
 
 }  // namespace qbc

@@ -35,7 +35,10 @@ template <bool EXACT, bool DYN, bool PROP = false>
 struct Walker {
   float3 p, d;   // ray origin and direction
   float3 inv;    // EXACT: RN(1 / d) per component (0 for a zero component)
-  bool fdiv;     // EXACT: plane hits divide by reciprocal (div_by_recip)
+  // EXACT: bit 0 plane hits divide by reciprocal (div_by_recip); bits 1, 2
+  // the candidates of the static / dynamic tree are filtered by the
+  // children's leaf boxes (child_box_hit)
+  uint32_t mode;
   float4 e0;     // entry point of the basecube (!EXACT; EXACT recomputes it)
   float4 cube;   // current cube (tlf.xyz, edge); !EXACT only
   uint32_t X, Y, Z;  // EXACT: path shift bits of the current cube, one per level
@@ -92,7 +95,7 @@ struct Walker {
   }
 
   // Start a ray: the basecube entry. Returns kDiscard or kRunning.
-  __device__ __forceinline__ int start(float4 bc, float3 rp, float3 rd) {
+  __device__ __forceinline__ int start(float4 bc, float3 rp, float3 rd, const DevScene& sc, int maxlevel) {
     p = rp;
     d = rd;
     cube = bc;
@@ -108,7 +111,17 @@ struct Walker {
     target = 0;
     tdepth = 0;
     if (EXACT) {
-      fdiv = recip_div_ok(p, d, bc.w);
+      const bool fdiv = recip_div_ok(p, d, bc.w);
+      // boxes: every direction component nonzero (finite reciprocals), the
+      // origin within 8 basecube edges (candidate points then stay within
+      // ~2^-17 S of the ray, far inside the 2^-14 S margin), and boxes built
+      // for a depth the render reaches
+      const float r8 = 8.0f * bc.w;
+      const bool geo = fdiv & (d.x != 0.0f) & (d.y != 0.0f) & (d.z != 0.0f) & (fabsf(p.x) <= r8) &
+                       (fabsf(p.y) <= r8) & (fabsf(p.z) <= r8);
+      const bool bs = geo & (sc.tree[0].cbox != nullptr) & (maxlevel >= sc.tree[0].box_depth);
+      const bool bd = DYN & geo & (sc.tree[1].cbox != nullptr) & (maxlevel >= sc.tree[1].box_depth);
+      mode = (fdiv ? 1u : 0u) | (bs ? 2u : 0u) | (bd ? 4u : 0u);
       inv = make_float3(d.x == 0.0f ? 0.0f : __frcp_rn(d.x), d.y == 0.0f ? 0.0f : __frcp_rn(d.y),
                         d.z == 0.0f ? 0.0f : __frcp_rn(d.z));
     }
@@ -213,13 +226,18 @@ struct Walker {
       }
     }
     // occupied octets: a child in either tree (:313-317)
-    uint32_t occ = 0;
+    uint32_t occ_s = 0, occ_d = 0;
 #pragma unroll
     for (int o = 0; o < 8; ++o) {
-      bool has = pick8(s0, s1, o) > 0;
-      if (DYN) has = has || pick8(d0, d1, o) > 0;
-      occ |= has ? (1u << o) : 0u;
+      occ_s |= pick8(s0, s1, o) > 0 ? (1u << o) : 0u;
+      if (DYN) occ_d |= pick8(d0, d1, o) > 0 ? (1u << o) : 0u;
     }
+    const uint32_t occ = occ_s | occ_d;
+    // leaf boxes of the children (EXACT rays that allow them)
+    const bool boxes = EXACT && (mode & 6u);
+    const float bm = bc.w * 6.1035156e-05f;  // margin 2^-14 S
+    const uint32_t* rec_s = (mode & 2u) ? sc.tree[0].cbox + (size_t)(uint32_t)ns * 16 : nullptr;
+    const uint32_t* rec_d = (DYN && (mode & 4u)) ? sc.tree[1].cbox + (size_t)(uint32_t)nd * 16 : nullptr;
     uint32_t pk = 0;
     int len = 0, pre = -1;
 #pragma unroll
@@ -244,6 +262,48 @@ struct Walker {
           ++len;
         }
       }
+    }
+    if (boxes && len > 0) {
+      // keep a candidate when a tree holding that child may have a leaf near
+      // the ray (one box at a time: a rolled loop keeps registers free)
+      uint32_t q = 0;
+      int nl = 0;
+      if constexpr (!DYN) {
+        // the records of all listed children first (independent loads), then
+        // the tests
+        uint2 ws[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          ws[k] = (k < len && rec_s) ? child_box_word(rec_s, (int)((pk >> (5 * k)) & 7u)) : make_uint2(0u, 0u);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          if (k < len) {
+            const uint32_t e = (pk >> (5 * k)) & 31u;
+            const int oct = (int)(e & 7u);
+            if (!rec_s || child_box_hit(ws[k], oct, cube, p, inv, bm)) {
+              q |= e << (5 * nl);
+              ++nl;
+            }
+          }
+        }
+      } else {
+        // two trees: one child at a time keeps the registers in bounds
+#pragma unroll 1
+        for (int k = 0; k < len; ++k) {
+          const uint32_t e = (pk >> (5 * k)) & 31u;
+          const int oct = (int)(e & 7u);
+          const bool hs = ((occ_s >> oct) & 1u) &&
+                          (!rec_s || child_box_hit(child_box_word(rec_s, oct), oct, cube, p, inv, bm));
+          const bool hd = ((occ_d >> oct) & 1u) &&
+                          (!rec_d || child_box_hit(child_box_word(rec_d, oct), oct, cube, p, inv, bm));
+          if (hs | hd) {
+            q |= e << (5 * nl);
+            ++nl;
+          }
+        }
+      }
+      pk = q;
+      len = nl;
     }
     pk |= (uint32_t)len << 20;
 

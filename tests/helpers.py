@@ -21,10 +21,14 @@ def bits(a: np.ndarray) -> np.ndarray:
     return np.ascontiguousarray(a).view(np.uint32)
 
 
-def compare_frame(gpu: dict, ref: dict, where: str = "") -> dict:
-    """Bit-exact comparison of every stream; returns counts for reporting."""
+def compare_frame(gpu: dict, ref: dict, where: str = "", visits: bool = False) -> dict:
+    """Bit-exact comparison of every stream; returns counts for reporting.
+    The per-pixel visit counts match the oracle's only with box pruning off
+    (QBC_OPT_BOX_PRUNE 0); visits=True compares them too."""
     key = {"rgba32f": "rgba"}
     for s in STREAMS:
+        if s == "visits" and not visits:
+            continue
         g = gpu[s]
         r = ref[key.get(s, s)]
         if s in ("rgba32f", "isp"):

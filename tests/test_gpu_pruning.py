@@ -1,0 +1,145 @@
+"""Leaf-box pruning (QBC_OPT_BOX_PRUNE): the walk skips children whose
+subtree's leaf box the ray misses. Every output stream but the per-pixel
+visit counts must equal the unpruned walk's (and so the oracle's); with
+pruning off the visit counts equal the oracle's too. Covered: the room scene,
+a dynamic tree, an inexact basecube, maxlevels below and above the tree's
+depth, rays, two-pass proposals, and edits after which the boxes are
+rebuilt."""
+import numpy as np
+import pytest
+
+from conftest import LEVELS, S
+from helpers import bits, compare_frame, gpu_frame, oracle_scene, upload_scene
+
+pytestmark = pytest.mark.gpu
+
+STREAMS = ("rgba8", "rgba32f", "flags", "leaf", "isp", "visits")
+
+
+@pytest.fixture
+def ctx():
+    import qubatron_gb300 as qb
+    c = qb.OctreeGLC(0)
+    yield c
+    c.close()
+
+
+def _views(sizes=((320, 200),), basesize=S, maxlevel=LEVELS, shoot=0):
+    from qubatron_gb300 import view_setup
+    poses = [((903.7, 421.3, 1702.9), (0.0, -0.3, 0.0), 0.0), ((500.2, 600.9, 1500.3), (-0.4, -0.45, 0.0), 1.1),
+             ((1300.5, 300.2, 400.7), (2.5, -0.2, 0.0), 2.0)]
+    return [view_setup(w, h, pos, ang, la, 10, maxlevel, basesize, shoot, 0.0)
+            for (w, h), (pos, ang, la) in zip(list(sizes) * len(poses), poses)]
+
+
+def _both(ctx, views, **kw):
+    import qubatron_gb300._lib as L
+    ctx.set_option(L.OPT_BOX_PRUNE, 1)
+    if kw:
+        on, _ = ctx.render_host_ex(views, STREAMS, **kw)
+    else:
+        on = ctx.render_host(views, STREAMS)
+    ctx.set_option(L.OPT_BOX_PRUNE, 0)
+    if kw:
+        off, _ = ctx.render_host_ex(views, STREAMS, **kw)
+    else:
+        off = ctx.render_host(views, STREAMS)
+    ctx.set_option(L.OPT_BOX_PRUNE, 1)
+    return on, off
+
+
+def _same_but_visits(on, off, where):
+    v_on = v_off = 0
+    for a, b in zip(on, off):
+        for k in STREAMS:
+            if k == "visits":
+                assert (a[k] <= b[k]).all(), f"{where}: a pruned walk visited more nodes"
+                v_on += int(a[k].astype(np.int64).sum())
+                v_off += int(b[k].astype(np.int64).sum())
+            else:
+                assert np.array_equal(a[k].view(np.uint8), b[k].view(np.uint8)), f"{where}: {k}"
+    return v_on, v_off
+
+
+def test_pruning_keeps_every_pixel_room(ctx):
+    from qubatron_gb300 import scenes
+    s = scenes.make_scene(scenes.scaled_spec("room20m", 400_000))
+    upload_scene(ctx, s.nodes, s.colors, s.normals)
+    v_on, v_off = _same_but_visits(*_both(ctx, _views()), "room")
+    assert v_on < 0.9 * v_off, (v_on, v_off)  # it prunes
+
+
+def test_pruning_with_dynamic_tree_and_two_pass(ctx, floor50k_scene):
+    from qubatron_gb300 import build_octree, scenes
+    import qubatron_gb300._lib as L
+    s = floor50k_scene
+    ch = scenes.make_character(40_000, root=(800.0, 60.0, 1100.0))
+    p, n = scenes.skin_reference(ch, scenes.pose_bones(ch, 1))
+    upload_scene(ctx, s.nodes, s.colors, s.normals, build_octree(p), ch.colors, n)
+    views = _views(shoot=1)
+    _same_but_visits(*_both(ctx, views), "dynamic")
+    _same_but_visits(*_both(ctx, views, two_pass=True), "two-pass")
+    ctx.render_host_ex(views, STREAMS, two_pass=True, log=True)
+    on, off = _both(ctx, views, two_pass=True, proposals=L.PROPOSE_LOGGED)
+    for a, b in zip(on, off):
+        for k in ("rgba8", "rgba32f", "flags", "isp"):
+            assert np.array_equal(a[k].view(np.uint8), b[k].view(np.uint8)), k
+
+
+def test_pruning_off_where_it_cannot_apply(ctx):
+    """An inexact basecube (no reciprocal walk), a maxlevel below the tree's
+    depth (boxes describe deeper leaves) and above it (nothing to hit)."""
+    from qubatron_gb300 import build_octree, scenes
+    bs = 1234.567
+    spec = scenes.scaled_spec("room20m", 150_000)
+    spec.basesize = bs
+    pts, nrm, col = scenes.generate_points(spec)
+    upload_scene(ctx, build_octree(pts, bs, LEVELS), col, nrm)
+    _same_but_visits(*_both(ctx, _views(basesize=bs)), "inexact basecube")
+    s = scenes.make_scene(scenes.scaled_spec("room20m", 150_000))
+    upload_scene(ctx, s.nodes, s.colors, s.normals)
+    for ml in (9, 11, 13):
+        _same_but_visits(*_both(ctx, _views(maxlevel=ml)), f"maxlevel {ml}")
+
+
+def test_pruning_rays_and_edits(ctx, floor50k_scene):
+    """Ray queries prune too; after removals, uploads and rebuilds the boxes
+    follow the tree."""
+    import qubatron_gb300._lib as L
+    s = floor50k_scene
+    upload_scene(ctx, s.nodes, s.colors, s.normals)
+    rng = np.random.default_rng(4)
+    pos = rng.uniform(0, S, (4000, 3)).astype(np.float32)
+    dirs = rng.normal(size=(4000, 3)).astype(np.float32)
+    base = (0.0, S, S, S)
+    got = {}
+    for prune in (1, 0):
+        ctx.set_option(L.OPT_BOX_PRUNE, prune)
+        got[prune] = ctx.trace_rays(pos, dirs, base, LEVELS)
+    ctx.set_option(L.OPT_BOX_PRUNE, 1)
+    for k in ("status", "leaf", "model"):
+        assert np.array_equal(got[1][k], got[0][k]), k
+    for k in ("isp", "col", "nrm"):
+        assert np.array_equal(bits(got[1][k]), bits(got[0][k])), k
+    views = _views()
+    ctx.render_host(views, ("rgba8",))  # boxes built
+    ctx.remove_points(False, s.points[::3])  # links cut: boxes stay conservative
+    _same_but_visits(*_both(ctx, views), "after removal")
+    ctx.build_tree(False, s.points[::2], S, LEVELS)  # rebuilt: boxes rebuilt
+    _same_but_visits(*_both(ctx, views), "after rebuild")
+    upload_scene(ctx, s.nodes, s.colors, s.normals)  # uploaded again
+    _same_but_visits(*_both(ctx, views), "after upload")
+
+
+def test_unpruned_visits_match_oracle(ctx, oracle, floor50k_scene):
+    """With pruning off the visit counts are the shader's, like every other
+    stream."""
+    import qubatron_gb300._lib as L
+    from qubatron_gb300 import view_setup
+    s = floor50k_scene
+    upload_scene(ctx, s.nodes, s.colors, s.normals)
+    ctx.set_option(L.OPT_BOX_PRUNE, 0)
+    sc = oracle_scene(oracle, s.nodes, s.colors, s.normals)
+    v = view_setup(320, 240, (903.7, 421.3, 1702.9), (0.0, -0.3, 0.0), 0.0, 10, LEVELS, S, 0, 0.0)
+    ov = oracle.QboView.from_bytes(v.to_bytes())
+    compare_frame(gpu_frame(ctx, v), oracle.render(sc, ov), "unpruned", visits=True)
