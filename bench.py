@@ -40,10 +40,12 @@ sys.path.insert(0, ROOT)
 WORKLOAD = "room20m_1920x1080x16"
 L2_BYTES = 129 * 1024 * 1024
 FALLBACK_HBM_GBS = 6800.0
-# algorithmic bytes: a node visit reads one 32-byte child
-# block of one tree; a leaf reads a 4-byte model index and a 12-byte colour
-# and 12-byte normal; every pixel writes 4 bytes of RGBA8
+# algorithmic bytes: a node visit reads one 32-byte child block of one tree;
+# the leaf-box filter reads one 8-byte word per tested child; a leaf reads a
+# 4-byte model index and a 12-byte colour and 12-byte normal; every pixel
+# writes 4 bytes of RGBA8
 BYTES_PER_VISIT = 32
+BYTES_PER_BOX_WORD = 8
 BYTES_PER_LEAF = 28
 BYTES_PER_PIXEL_OUT = 4
 
@@ -416,10 +418,10 @@ def run_gpu(args):
         o.flags = fl.data_ptr()
         o.visits = vi.data_ptr()
         inst.append(o)
-    frame_rays, frame_bytes = [], []
+    frame_rays, frame_bytes, frame_visits, frame_words = [], [], [], []
     for k in range(args.steps if chars else 1):
         update(args.warmup + k)
-        ctx.render_views(views, inst, on_device=True)
+        words_k = ctx.render_views_ex(views, inst, on_device=True)["box_words"]
         torch.cuda.synchronize()
         rays_k, vis_k, leaves_k = 0, 0, 0
         for fl, vi in zip(flags, visits):
@@ -429,7 +431,10 @@ def run_gpu(args):
             vis_k += int(vi.to(torch.int64).sum().item())
         pixels = sum(v.width_px * v.height_px for v in views)
         frame_rays.append(rays_k)
-        frame_bytes.append(vis_k * BYTES_PER_VISIT + leaves_k * BYTES_PER_LEAF + pixels * BYTES_PER_PIXEL_OUT)
+        frame_visits.append(vis_k)
+        frame_words.append(words_k)
+        frame_bytes.append(vis_k * BYTES_PER_VISIT + words_k * BYTES_PER_BOX_WORD + leaves_k * BYTES_PER_LEAF
+                           + pixels * BYTES_PER_PIXEL_OUT)
     if not chars:
         frame_rays *= args.steps
         frame_bytes *= args.steps
@@ -535,7 +540,9 @@ def run_gpu(args):
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "peak_kind": f"{peak_kind} (burst copy)",
-                     "algorithmic_bytes_per_launch": alg_bytes},
+                     "algorithmic_bytes_per_launch": alg_bytes,
+                     "node_visits_per_launch": statistics.mean(frame_visits),
+                     "box_words_per_launch": statistics.mean(frame_words)},
         "clocks": clk.summary(),
         "step_ms": [round(x, 4) for x in step_ms],
     }

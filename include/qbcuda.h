@@ -235,7 +235,10 @@ int qbc_trace_rays(qbc_ctx* ctx, const float* pos, const float* dir, int64_t n, 
  * overlaps on the GPU (different streams, different contexts on one device)
  * race and must be ordered by the caller. The first call on a device looks
  * up the array's device address; make that first call before any stream
- * capture. Host output pointers are rejected with QBC_E_ARG.
+ * capture. Host output pointers are rejected with QBC_E_ARG. Building leaf
+ * boxes (QBC_OPT_BOX_PRUNE) allocates, so this call never builds them: it
+ * prunes with the boxes an earlier allocating render built for the current
+ * trees, and walks a tree changed since then unpruned (same pixels).
  */
 #define QBC_NOALLOC_MAX_LAUNCHES 8
 #define QBC_NOALLOC_MAX_VIEWS (QBC_NOALLOC_MAX_LAUNCHES * 32)
@@ -278,7 +281,10 @@ typedef struct qbc_render_opts
     uint64_t seed;
 } qbc_render_opts;
 
-/* Counters of the last qbc_render_views_ex call (two_pass only). */
+/* Counters of the last qbc_render_views_ex call. The first six count the
+ * shade pass of a two_pass render (0 otherwise); box_words counts the 8-byte
+ * leaf-box words (QBC_OPT_BOX_PRUNE) read by all walks of a render in which a
+ * view has a visits output (0 otherwise). */
 typedef struct qbc_render_stats
 {
     uint64_t queued;            /* pixels in the shade pass */
@@ -287,6 +293,7 @@ typedef struct qbc_render_stats
     uint64_t proposals_tried;   /* proposal walks */
     uint64_t proposals_proven;  /* shadow rays settled by a proposal */
     uint64_t proposal_visits;   /* node visits of proposal walks */
+    uint64_t box_words;         /* leaf-box words read (instrumented renders) */
 } qbc_render_stats;
 
 int qbc_render_views_ex(qbc_ctx* ctx, const qbc_view* views, const qbc_outputs* outs, int n, int outputs_on_device, const qbc_render_opts* opts, qbc_render_stats* stats);

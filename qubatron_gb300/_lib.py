@@ -123,6 +123,7 @@ class RenderStats(C.Structure):
         ("proposals_tried", C.c_uint64),
         ("proposals_proven", C.c_uint64),
         ("proposal_visits", C.c_uint64),
+        ("box_words", C.c_uint64),
     ]
 
     def as_dict(self) -> dict:

@@ -121,6 +121,7 @@ inline int launch_grid(const qbc_ctx* c, int64_t n) {
 
 inline qbc::DevScene device_scene(const qbc_ctx* c) {
   qbc::DevScene s;
+  s.box_words = nullptr;
   for (int t = 0; t < 2; ++t) {
     s.tree[t].child = c->tree[t].child;
     s.tree[t].model = c->tree[t].model;

@@ -662,13 +662,14 @@ void** out_slot(qbc_outputs& o, int k) {
 }
 
 
-// Statistics of the shade passes of the last two-pass render (synchronizes).
-int read_stats(qbc_ctx* c, qbc_render_stats* stats) {
+// Statistics of the last render: the shade passes' counters of a two-pass
+// render, the leaf-box words of an instrumented one (synchronizes).
+int read_stats(qbc_ctx* c, qbc_render_stats* stats, bool two) {
   if (!stats) return QBC_OK;
   unsigned long long h[qbc::kStatCount];
-  unsigned int q[2];
+  unsigned int q[2] = {0u, 0u};
   QBC_CUDA(cudaMemcpyAsync(h, c->wstats, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
-  QBC_CUDA(cudaMemcpyAsync(q, c->wcount, sizeof(q), cudaMemcpyDeviceToHost, c->stream));
+  if (two) QBC_CUDA(cudaMemcpyAsync(q, c->wcount, sizeof(q), cudaMemcpyDeviceToHost, c->stream));
   QBC_CUDA(cudaStreamSynchronize(c->stream));
   stats->queued = q[0];
   stats->shadow_rays = h[qbc::kStatShadowRays];
@@ -676,6 +677,7 @@ int read_stats(qbc_ctx* c, qbc_render_stats* stats) {
   stats->proposals_tried = h[qbc::kStatPropTried];
   stats->proposals_proven = h[qbc::kStatPropProven];
   stats->proposal_visits = h[qbc::kStatPropVisits];
+  stats->box_words = h[qbc::kStatBoxWords];
   return QBC_OK;
 }
 
@@ -697,7 +699,10 @@ int launch_render(qbc_ctx* c, const qbc::Batch& b, size_t smem, const qbc::Wave&
   if (MODE != qbc::kShadePass) blocks = std::min<int64_t>(blocks, ((int64_t)b.tiles_total + 3) / 4);
   blocks = std::max<int64_t>(blocks, 1);
   if (MODE != qbc::kShadePass) QBC_CUDA(cudaMemsetAsync(c->queue, 0, sizeof(unsigned int), c->stream));
-  kern<<<(unsigned)blocks, qbc::kThreads, smem, c->stream>>>(device_scene(c), b, c->queue, wave);
+  qbc::DevScene sc = device_scene(c);
+  for (int i = 0; i < b.n; ++i)
+    if (b.job[i].o.visits) sc.box_words = c->wstats + qbc::kStatBoxWords;  // an instrumented render
+  kern<<<(unsigned)blocks, qbc::kThreads, smem, c->stream>>>(sc, b, c->queue, wave);
   QBC_CUDA(cudaGetLastError());
   ++c->launches;
   return QBC_OK;
@@ -831,13 +836,13 @@ int render_views_impl(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs
   int brc = ensure_boxes(c);
   if (brc) return brc;
   const bool two = opts && opts->two_pass;
-  if (two) QBC_CUDA(cudaMemsetAsync(c->wstats, 0, qbc::kStatCount * sizeof(unsigned long long), c->stream));
+  if (two || stats) QBC_CUDA(cudaMemsetAsync(c->wstats, 0, qbc::kStatCount * sizeof(unsigned long long), c->stream));
   if (outputs_on_device) {
     for (int a = 0; a < n; a += qbc::kMaxViewsPerLaunch) {
       int rc = launch_batch(c, views + a, outs + a, std::min(qbc::kMaxViewsPerLaunch, n - a), opts);
       if (rc) return rc;
     }
-    return two ? read_stats(c, stats) : QBC_OK;
+    return read_stats(c, stats, two);
   }
 
   // host outputs: render into device scratch, then copy each stream back
@@ -882,7 +887,7 @@ int render_views_impl(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs
     }
   }
   QBC_CUDA(cudaStreamSynchronize(c->stream));
-  return two ? read_stats(c, stats) : QBC_OK;
+  return read_stats(c, stats, two);
 }
 
 extern "C" int qbc_trace_rays(qbc_ctx* c, const float* pos, const float* dir, int64_t n, const float basecube[4],

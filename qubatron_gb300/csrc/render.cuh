@@ -97,13 +97,15 @@ constexpr int kRecLogLit = kRecLogT + 1;  // lit bit of the plain shadow walk
 enum Phase : int { kIdle = 0, kPrimary = 1, kShadow = 2, kFlare = 3, kProposal = 4 };
 enum Mode : int { kFused = 0, kPrimaryPass = 1, kShadePass = 2 };
 
-// Statistics of the shade pass (uint64 each).
+// Statistics of a render (uint64 each): the shade pass's counters, and the
+// leaf-box words read by the walks of an instrumented render.
 enum Stat : int {
   kStatShadowRays = 0,   // plain shadow walks
   kStatShadowVisits,     // node visits of plain shadow walks
   kStatPropTried,        // proposal walks
   kStatPropProven,       // shadow rays settled by a proposal
   kStatPropVisits,       // node visits of proposal walks
+  kStatBoxWords,         // leaf-box words read (renders with a visits output)
   kStatCount = 8
 };
 

@@ -49,6 +49,7 @@ struct DevModel {
 struct DevScene {
   DevTree tree[2];    // 0 static, 1 dynamic
   DevModel model[2];
+  unsigned long long* box_words;  // when set: add the leaf-box words the walks read
 };
 
 enum : int { kMiss = 0, kLeaf = 1, kDiscard = 2 };
@@ -278,15 +279,17 @@ __device__ __forceinline__ int list_next(uint32_t pk) { return (pk >> 23) & 7; }
 __device__ __forceinline__ int list_entry(uint32_t pk, int k) { return (pk >> (5 * k)) & 31; }
 
 
-// Whether the ray p + t d (t >= 0) passes within m of the leaf box of child o
-// (its record word r, boxes.cu) of the node whose cube is
-// `cube`. inv = 1 / d with no zero component. A miss proves that the walk
-// finds no leaf below that child: every candidate point it computes lies
-// within a small multiple of the coordinates' ulp of the ray, far below m,
-// and a leaf is only reached through a point inside it.
+// Record word of child o in a node's leaf-box record (boxes.cu).
 __device__ __forceinline__ uint2 child_box_word(const uint32_t* rec, int o) {
   return __ldg(reinterpret_cast<const uint2*>(rec) + o);
 }
+
+// Whether the ray p + t d (t >= 0) passes within m of the leaf box of child o
+// (its record word r) of the node whose cube is `cube`. inv = 1 / d with no
+// zero component. A miss proves that the walk finds no leaf below that child:
+// every candidate point it computes lies within a small multiple of the
+// coordinates' ulp of the ray, far below m, and a leaf is only reached
+// through a point inside it.
 __device__ __forceinline__ bool child_box_hit(uint2 r, int o, float4 cube, float3 p, float3 inv, float m) {
   const uint32_t a = r.x, b = r.y;
   // byte k of w as a float: bits 0x4B0000kk are 2^23 + k

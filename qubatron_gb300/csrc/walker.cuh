@@ -265,7 +265,19 @@ struct Walker {
     }
     if (boxes && len > 0) {
       // keep a candidate when a tree holding that child may have a leaf near
-      // the ray (one box at a time: a rolled loop keeps registers free)
+      // the ray
+      if (sc.box_words) {
+        // instrumented renders: the box words the filter reads
+        uint32_t nw = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const uint32_t bit = 1u << ((pk >> (5 * k)) & 7u);
+          if (k < len) nw += ((occ_s & bit) && rec_s ? 1u : 0u) + ((occ_d & bit) && rec_d ? 1u : 0u);
+        }
+        const unsigned m = __activemask();
+        const unsigned tot = __reduce_add_sync(m, nw);
+        if ((int)(threadIdx.x & 31u) == __ffs((int)m) - 1) atomicAdd(sc.box_words, (unsigned long long)tot);
+      }
       uint32_t q = 0;
       int nl = 0;
       if constexpr (!DYN) {

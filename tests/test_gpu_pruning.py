@@ -143,3 +143,35 @@ def test_unpruned_visits_match_oracle(ctx, oracle, floor50k_scene):
     v = view_setup(320, 240, (903.7, 421.3, 1702.9), (0.0, -0.3, 0.0), 0.0, 10, LEVELS, S, 0, 0.0)
     ov = oracle.QboView.from_bytes(v.to_bytes())
     compare_frame(gpu_frame(ctx, v), oracle.render(sc, ov), "unpruned", visits=True)
+
+
+def test_box_word_counter(ctx, floor50k_scene):
+    """qbc_render_stats.box_words: the leaf-box words the walks read, counted
+    on renders with a visits output and pruning on; at most one word per
+    listed child (four per node visit of the static tree, eight with a
+    dynamic tree as well)."""
+    from qubatron_gb300 import build_octree, scenes
+    import qubatron_gb300._lib as L
+    s = scenes.make_scene(scenes.scaled_spec("room20m", 300_000))
+    upload_scene(ctx, s.nodes, s.colors, s.normals)
+    views = _views()
+    ctx.set_option(L.OPT_BOX_PRUNE, 1)
+    bufs, st = ctx.render_host_ex(views, ("rgba8", "visits"))
+    visits = sum(int(b["visits"].astype(np.int64).sum()) for b in bufs)
+    assert 0 < st["box_words"] <= 4 * visits, (st["box_words"], visits)
+    assert st["queued"] == 0 and st["shadow_rays"] == 0  # a fused render
+    _, st = ctx.render_host_ex(views, ("rgba8",))
+    assert st["box_words"] == 0  # not instrumented
+    ctx.set_option(L.OPT_BOX_PRUNE, 0)
+    _, st = ctx.render_host_ex(views, ("rgba8", "visits"))
+    assert st["box_words"] == 0  # no boxes
+    ctx.set_option(L.OPT_BOX_PRUNE, 1)
+    f = floor50k_scene
+    ch = scenes.make_character(40_000, root=(800.0, 60.0, 1100.0))
+    p, n = scenes.skin_reference(ch, scenes.pose_bones(ch, 1))
+    upload_scene(ctx, f.nodes, f.colors, f.normals, build_octree(p), ch.colors, n)
+    views = _views(shoot=1)
+    bufs, st = ctx.render_host_ex(views, ("rgba8", "visits"), two_pass=True)
+    visits = sum(int(b["visits"].astype(np.int64).sum()) for b in bufs)
+    assert 0 < st["box_words"] <= 8 * visits, (st["box_words"], visits)
+    assert st["shadow_rays"] > 0
