@@ -284,37 +284,65 @@ __device__ __forceinline__ uint2 child_box_word(const uint32_t* rec, int o) {
   return __ldg(reinterpret_cast<const uint2*>(rec) + o);
 }
 
-// Whether the ray p + t d (t >= 0) passes within m of the leaf box of child o
-// (its record word r) of the node whose cube is `cube`. inv = 1 / d with no
-// zero component. A miss proves that the walk finds no leaf below that child:
-// every candidate point it computes lies within a small multiple of the
+// Whether the ray p + t d (t >= 0) passes within m of the leaf box of a
+// child. A miss proves that the walk finds no leaf below that child: every
+// candidate point it computes lies within a small multiple of the
 // coordinates' ulp of the ray, far below m, and a leaf is only reached
 // through a point inside it.
-__device__ __forceinline__ bool child_box_hit(uint2 r, int o, float4 cube, float3 p, float3 inv, float m) {
-  const uint32_t a = r.x, b = r.y;
-  // byte k of w as a float: bits 0x4B0000kk are 2^23 + k
-  auto f8 = [](uint32_t w, uint32_t sel) { return __uint_as_float(__byte_perm(w, 0x4B000000u, sel)) - 8388608.0f; };
-  const float xlo = f8(a, 0x7540u), xhi = f8(a, 0x7541u), ylo = f8(a, 0x7542u), yhi = f8(a, 0x7543u);
-  const float zlo = f8(b, 0x7540u), zhi = f8(b, 0x7541u);
-  const float half = cube.w * 0.5f, unit = half * 0.00390625f;  // 1/256 of the child's edge
-  const float x0 = cube.x + ((o & 1) ? half : 0.0f);
-  const float y0 = cube.y - ((o & 2) ? half : 0.0f);
-  const float z0 = cube.z - ((o & 4) ? half : 0.0f);
-  // world bounds (y and z counted downward from the child's top), widened by m
-  const float bx0 = __fmaf_rn(xlo, unit, x0 - m), bx1 = __fmaf_rn(xhi + 1.0f, unit, x0 + m);
-  const float by0 = __fmaf_rn(-(yhi + 1.0f), unit, y0 - m), by1 = __fmaf_rn(-ylo, unit, y0 + m);
-  const float bz0 = __fmaf_rn(-(zhi + 1.0f), unit, z0 - m), bz1 = __fmaf_rn(-zlo, unit, z0 + m);
-  float t0 = (bx0 - p.x) * inv.x, t1 = (bx1 - p.x) * inv.x;
+//
+// BoxFrame holds what the test of all children of one node shares: per axis
+// the ray's t at the node's x-min (y-max, z-max) face moved outward by -m
+// (a0) and +m (a1) along that axis, and the change of t per box unit (1/256
+// of a child's edge) into the cube (u; y and z count downward). A bound q
+// units into the cube is then one FMA: a + q * u. Against the direct slab
+// test this regroups (c + q * unit +- m - p) / d; the extra rounding is a
+// few ulps of coordinates below 9 S, about 2^-20 S, far inside m = 2^-14 S.
+struct BoxFrame {
+  float a0[3], a1[3], u[3];
+};
+__device__ __forceinline__ BoxFrame box_frame(float4 cube, float3 p, float3 inv, float m) {
+  const float unit = cube.w * 0.001953125f;  // 1/512 of the node's edge
+  BoxFrame f;
+  const float ax = (cube.x - p.x) * inv.x, mx = m * inv.x;
+  const float ay = (cube.y - p.y) * inv.y, my = m * inv.y;
+  const float az = (cube.z - p.z) * inv.z, mz = m * inv.z;
+  f.a0[0] = ax - mx;
+  f.a1[0] = ax + mx;
+  f.u[0] = unit * inv.x;
+  f.a0[1] = ay - my;
+  f.a1[1] = ay + my;
+  f.u[1] = -(unit * inv.y);
+  f.a0[2] = az - mz;
+  f.a1[2] = az + mz;
+  f.u[2] = -(unit * inv.z);
+  return f;
+}
+
+// Test of child o with its record word r (boxes.cu: bytes xlo xhi ylo yhi,
+// then zlo zhi, in units from the child's x-min, y-max, z-max corner).
+__device__ __forceinline__ bool child_box_hit(uint2 r, int o, const BoxFrame& f) {
+  // byte k of w as a float: bits 0x4B0000kk are 2^23 + k; subtracting
+  // 2^23 - c gives k + c exactly (c: the child's offset of 256 units in the
+  // node, plus 1 for a high bound's far side)
+  auto q = [](uint32_t w, uint32_t sel, float k) { return __uint_as_float(__byte_perm(w, 0x4B000000u, sel)) - k; };
+  const float kx = (o & 1) ? 8388352.0f : 8388608.0f, ky = (o & 2) ? 8388352.0f : 8388608.0f,
+              kz = (o & 4) ? 8388352.0f : 8388608.0f;
+  const float xlo = q(r.x, 0x7540u, kx), xhi = q(r.x, 0x7541u, kx - 1.0f);
+  const float ylo = q(r.x, 0x7542u, ky), yhi = q(r.x, 0x7543u, ky - 1.0f);
+  const float zlo = q(r.y, 0x7540u, kz), zhi = q(r.y, 0x7541u, kz - 1.0f);
+  // x: low bound - m, high bound + m; y and z run downward, so their high
+  // bound is the low coordinate
+  float t0 = __fmaf_rn(xlo, f.u[0], f.a0[0]), t1 = __fmaf_rn(xhi, f.u[0], f.a1[0]);
   float tn = fminf(t0, t1), tf = fmaxf(t0, t1);
-  t0 = (by0 - p.y) * inv.y;
-  t1 = (by1 - p.y) * inv.y;
+  t0 = __fmaf_rn(yhi, f.u[1], f.a0[1]);
+  t1 = __fmaf_rn(ylo, f.u[1], f.a1[1]);
   tn = fmaxf(tn, fminf(t0, t1));
   tf = fminf(tf, fmaxf(t0, t1));
-  t0 = (bz0 - p.z) * inv.z;
-  t1 = (bz1 - p.z) * inv.z;
+  t0 = __fmaf_rn(zhi, f.u[2], f.a0[2]);
+  t1 = __fmaf_rn(zlo, f.u[2], f.a1[2]);
   tn = fmaxf(tn, fminf(t0, t1));
   tf = fminf(tf, fmaxf(t0, t1));
-  return (xlo <= xhi) & (tn <= tf) & (tf >= 0.0f);  // xlo > xhi: a subtree without leaves
+  return (xlo < xhi) & (tn <= tf) & (tf >= 0.0f);  // xlo >= xhi + 1: a subtree without leaves
 }
 
 }  // namespace qbc

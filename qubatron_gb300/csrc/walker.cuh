@@ -234,10 +234,13 @@ struct Walker {
     }
     const uint32_t occ = occ_s | occ_d;
     // leaf boxes of the children (EXACT rays that allow them)
-    const bool boxes = EXACT && (mode & 6u);
-    const float bm = bc.w * 6.1035156e-05f;  // margin 2^-14 S
-    const uint32_t* rec_s = (mode & 2u) ? sc.tree[0].cbox + (size_t)(uint32_t)ns * 16 : nullptr;
-    const uint32_t* rec_d = (DYN && (mode & 4u)) ? sc.tree[1].cbox + (size_t)(uint32_t)nd * 16 : nullptr;
+    // (not one level above the tree's deepest: a child there is a leaf
+    // cell, its box the whole child cube, which every listed child meets)
+    const bool box_s = EXACT && (mode & 2u) && level + 1 < sc.tree[0].box_depth;
+    const bool box_d = EXACT && DYN && (mode & 4u) && level + 1 < sc.tree[1].box_depth;
+    const bool boxes = box_s || box_d;
+    const uint32_t* rec_s = box_s ? sc.tree[0].cbox + (size_t)(uint32_t)ns * 16 : nullptr;
+    const uint32_t* rec_d = box_d ? sc.tree[1].cbox + (size_t)(uint32_t)nd * 16 : nullptr;
     uint32_t pk = 0;
     int len = 0, pre = -1;
 #pragma unroll
@@ -278,6 +281,7 @@ struct Walker {
         const unsigned tot = __reduce_add_sync(m, nw);
         if ((int)(threadIdx.x & 31u) == __ffs((int)m) - 1) atomicAdd(sc.box_words, (unsigned long long)tot);
       }
+      const BoxFrame bf = box_frame(cube, p, inv, bc.w * 6.1035156e-05f);  // margin 2^-14 S
       uint32_t q = 0;
       int nl = 0;
       if constexpr (!DYN) {
@@ -292,7 +296,7 @@ struct Walker {
           if (k < len) {
             const uint32_t e = (pk >> (5 * k)) & 31u;
             const int oct = (int)(e & 7u);
-            if (!rec_s || child_box_hit(ws[k], oct, cube, p, inv, bm)) {
+            if (!rec_s || child_box_hit(ws[k], oct, bf)) {
               q |= e << (5 * nl);
               ++nl;
             }
@@ -305,9 +309,9 @@ struct Walker {
           const uint32_t e = (pk >> (5 * k)) & 31u;
           const int oct = (int)(e & 7u);
           const bool hs = ((occ_s >> oct) & 1u) &&
-                          (!rec_s || child_box_hit(child_box_word(rec_s, oct), oct, cube, p, inv, bm));
+                          (!rec_s || child_box_hit(child_box_word(rec_s, oct), oct, bf));
           const bool hd = ((occ_d >> oct) & 1u) &&
-                          (!rec_d || child_box_hit(child_box_word(rec_d, oct), oct, cube, p, inv, bm));
+                          (!rec_d || child_box_hit(child_box_word(rec_d, oct), oct, bf));
           if (hs | hd) {
             q |= e << (5 * nl);
             ++nl;
