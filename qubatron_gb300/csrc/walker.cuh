@@ -210,20 +210,30 @@ struct Walker {
       c[3] = s3 ? cy : 0u;
     }
     const int hc = 1 + (int)vz + (int)vx + (int)vy;
-    // ordering by swaps, as the shader's nested loop (:276-290)
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-#pragma unroll
-      for (int j = i + 1; j < 4; ++j) {
-        if (t[j] < t[i]) {
-          float tt = t[i];
-          t[i] = t[j];
-          t[j] = tt;
-          uint32_t cc = c[i];
-          c[i] = c[j];
-          c[j] = cc;
-        }
+    // ordering by swaps, as the shader's nested loop (:276-290). When no
+    // plane hit's t is below the entry's (the rule, unless the entry lies on
+    // a bisecting plane) the first pass swaps nothing and the passes left are
+    // the same network on slots 1..3; the warp takes that path when all its
+    // lanes can.
+    auto order = [&](int i, int j) {
+      if (t[j] < t[i]) {
+        float tt = t[i];
+        t[i] = t[j];
+        t[j] = tt;
+        uint32_t cc = c[i];
+        c[i] = c[j];
+        c[j] = cc;
       }
+    };
+    if (__all_sync(__activemask(), t[0] <= fminf(t[1], fminf(t[2], t[3])))) {
+      order(1, 2);
+      order(1, 3);
+      order(2, 3);
+    } else {
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = i + 1; j < 4; ++j) order(i, j);
     }
     // occupied octets: a child in either tree (:313-317)
     uint32_t occ_s = 0, occ_d = 0;
@@ -339,9 +349,10 @@ struct Walker {
     int cc;
     if (len > 0) {
       // ---- descend into the nearest candidate (:334-367) ----
+      // (a plane hit is recomputed below from its source, with the same
+      // operations: cheaper than keeping all three live through the filter)
       cc = PROP ? list_entry(pk, nx) : (int)(pk & 31);
-      int src = cc >> 3;
-      isp = src == 0 ? e : (src == 1 ? hz : (src == 2 ? hx : hy));
+      isp = e;
       cs = pick8(s0, s1, cc & 7);
       if (DYN) cd = pick8(d0, d1, cc & 7);
       slot(st, level, 1) = (uint32_t)ns;
@@ -371,24 +382,26 @@ struct Walker {
         }
       }
       cc = list_entry(pk, nx);
-      int src = cc >> 3;
-      if (!EXACT || src == 0) {
+      if (!EXACT || (cc >> 3) == 0) {
         float4 rc, re;
         replay_to(st, level, bc, rc, re);
         cube = rc;
         isp = re;
-      }
-      if (src != 0) {
-        if (EXACT && fast)
-          isp = plane_point_rcp(src, cube, p, d, inv);
-        else
-          isp = plane_point(src, cube, p, d);
       }
       int32_t ps = (int32_t)slot(st, level, 1);
       cs = load_child(sc.tree[0], ps, level, cc & 7, oob);
       if (DYN) {
         int32_t pd = (int32_t)slot(st, level, 2);
         cd = load_child(sc.tree[1], pd, level, cc & 7, oob);
+      }
+    }
+    {
+      const int src = cc >> 3;
+      if (src != 0) {
+        if (EXACT && fast)
+          isp = plane_point_rcp(src, cube, p, d, inv);
+        else
+          isp = plane_point(src, cube, p, d);
       }
     }
     if (++pushes > kMaxPushes) {
