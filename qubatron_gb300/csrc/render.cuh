@@ -71,6 +71,14 @@ __device__ __forceinline__ float4 view_bc(const qbc_view& v) {
   return make_float4(v.basecube[0], v.basecube[1], v.basecube[2], v.basecube[3]);
 }
 
+// The basecube as the kernels hold it: an EXACT launch has only views with
+// basecube (+0, S, S, S) (cube_shift_exact), so one register holds it.
+template <bool EXACT>
+__device__ __forceinline__ float4 held_bc(const qbc_view& v) {
+  const float s = v.basecube[3];
+  return EXACT ? make_float4(0.0f, s, s, s) : view_bc(v);
+}
+
 // Per-lane pixel state in shared memory, word k at px[k * kThreads]. The
 // first kRecCopy words are also the record a primary pass hands to the
 // shade pass.
@@ -211,7 +219,7 @@ struct Shader {
     px.w(kPxXY) = (uint32_t)i | ((uint32_t)j << 16);
     const qbc_view& v = batch.job[vi].v;
     maxlevel = v.maxlevel;
-    bc = view_bc(v);
+    bc = held_bc<EXACT>(v);
     float cx = ((float)i + 0.5f) * v.coord_scale[0];
     float cy = ((float)j + 0.5f) * v.coord_scale[1];
     float3 csv = make_float3(cx - v.cfp[0], cy - v.cfp[1], 0.0f - v.cfp[2]);
@@ -269,7 +277,7 @@ struct Shader {
     rec_q = q;
     const qbc_view& v = view();
     maxlevel = v.maxlevel;
-    bc = view_bc(v);
+    bc = held_bc<EXACT>(v);
     prop_k = 0;
     next_tdepth = 0;
     if (px.w(kPxFlags) & QBC_PX_SHADED) {
@@ -437,6 +445,13 @@ struct Shader {
   }
 };
 
+// Lanes below this one in the warp (a special register: nothing held).
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
 // Global tile queue: 32-pixel warp tiles (8x4 by default), numbered view by
 // view.
 __device__ __forceinline__ int tile_view(const Batch& b, int tile) {
@@ -462,8 +477,16 @@ constexpr int kServiceMinDefault = 4;
 // record queue (warp-aggregated atomics), the rest are written.
 // MODE kShadePass: the queued pixels' shadow rays (first the proposals, with
 // PROP), shading and flare.
+// Minimum resident blocks per SM the register allocation must allow: the
+// walk is latency-bound per warp, so more resident warps pay as long as
+// nothing spills (static tree: 6, 80 registers; both trees: 5, 96).
+template <bool DYN, int MODE>
+constexpr int render_min_blocks() {
+  return DYN ? 5 : (MODE == kShadePass ? 1 : 6);
+}
+
 template <bool EXACT, bool DYN, int MODE, bool PROP>
-__global__ void __launch_bounds__(kThreads, DYN ? 5 : 1) render_kernel(DevScene sc, const __grid_constant__ Batch batch,
+__global__ void __launch_bounds__(kThreads, render_min_blocks<DYN, MODE>()) render_kernel(DevScene sc, const __grid_constant__ Batch batch,
                                                           unsigned int* queue, const __grid_constant__ Wave wave) {
   extern __shared__ uint32_t smem[];
   const int tid = threadIdx.x, lane = tid & 31;
@@ -485,7 +508,6 @@ __global__ void __launch_bounds__(kThreads, DYN ? 5 : 1) render_kernel(DevScene 
   int chunk = 0, consumed = 32;  // warp-uniform
   bool fast = false;             // warp-uniform: see the service phase
   bool exhausted = false;
-  const unsigned lt_mask = (1u << lane) - 1u;
   const unsigned total = MODE == kShadePass ? min(*wave.qcount, wave.cap) : (unsigned)batch.tiles_total;
 
   for (;;) {
@@ -504,7 +526,7 @@ __global__ void __launch_bounds__(kThreads, DYN ? 5 : 1) render_kernel(DevScene 
           if (lane == __ffs(enq) - 1) base = atomicAdd(wave.qcount, (unsigned)__popc(enq));
           base = __shfl_sync(0xFFFFFFFFu, base, __ffs(enq) - 1);
           if (S.enqueue) {
-            const unsigned q = base + __popc(enq & lt_mask);
+            const unsigned q = base + __popc(enq & lanemask_lt());
             if (q < wave.cap) {
               uint32_t* r = wave.rec + (size_t)q * kRecWords;
 #pragma unroll
@@ -528,7 +550,7 @@ __global__ void __launch_bounds__(kThreads, DYN ? 5 : 1) render_kernel(DevScene 
           }
         }
         const int avail = 32 - consumed;
-        const int rank = __popc(idle & lt_mask);
+        const int rank = __popc(idle & lanemask_lt());
         if (((idle >> lane) & 1u) && rank < avail) {
           const int slot = consumed + rank;
           if (MODE == kShadePass) {

@@ -353,8 +353,14 @@ struct Walker {
       // operations: cheaper than keeping all three live through the filter)
       cc = PROP ? list_entry(pk, nx) : (int)(pk & 31);
       isp = e;
-      cs = pick8(s0, s1, cc & 7);
-      if (DYN) cd = pick8(d0, d1, cc & 7);
+      if (DYN) {
+        cs = pick8(s0, s1, cc & 7);
+        cd = pick8(d0, d1, cc & 7);
+      } else {
+        // the static-tree kernels read the child again (an L1 hit) rather
+        // than keep the block's 8 registers live: 6 blocks per SM fit
+        cs = load_child(sc.tree[0], ns, level, cc & 7, oob);
+      }
       slot(st, level, 1) = (uint32_t)ns;
       if (DYN) slot(st, level, 2) = (uint32_t)nd;
     } else {
