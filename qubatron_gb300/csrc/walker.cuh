@@ -185,21 +185,34 @@ struct Walker {
     bool vy = (d.y != 0.0f) & (hy.w > 0.0f) & in_yface(hy, cube, cb);
 
     // Candidates in the shader's fill order (entry, z, x, y), compacted, as
-    // (t, code): code = octet side bits | source << 3. A bisecting-plane hit
-    // lies on its own plane (its coordinate is the midpoint itself), so its
-    // side bit on that axis is 0. Unused slots hold t = +inf: a valid
-    // candidate has a finite t, so the ordering below never swaps a pad.
+    // (t, code): code = octet side bits | source << 3 | flip << 5. A
+    // bisecting-plane hit lies on its own plane (its coordinate is the
+    // midpoint itself), so its side bit on that axis is 0. Unused slots hold
+    // t = +inf: a valid candidate has a finite t, so the ordering below never
+    // swaps a pad.
+    //
+    // flip is the octet bit the pair fix-up (:301-309) toggles when the point
+    // falls in the same octet as the candidate before it: the first axis, x
+    // then y then z, on which the point equals the midpoint. A plane hit
+    // always equals it on its own axis, so an x hit flips x, a y hit x or
+    // y, a z hit x, y or z; only the entry point may flip nothing. The
+    // fix-up is common (a ray crossing a bisecting plane towards its high
+    // side meets it), so the flips are found here, where the points are at
+    // hand, instead of in a branch per candidate.
     const float kInf = __int_as_float(0x7f800000);
     float t[4];
     uint32_t c[4];
     t[0] = e.w;
-    c[0] = (e.x > hl.x ? 1u : 0u) | (e.y < hl.y ? 2u : 0u) | (e.z < hl.z ? 4u : 0u);
+    c[0] = (e.x > hl.x ? 1u : 0u) | (e.y < hl.y ? 2u : 0u) | (e.z < hl.z ? 4u : 0u) |
+           (e.x == hl.x ? 1u << 5 : (e.y == hl.y ? 2u << 5 : (e.z == hl.z ? 4u << 5 : 0u)));
     {
       // the valid plane hits fill slots 1.. in the order z, x, y (selects:
       // the lanes of a warp differ in which hits are valid)
-      const uint32_t cz = (hz.x > hl.x ? 1u : 0u) | (hz.y < hl.y ? 2u : 0u) | (1u << 3);
-      const uint32_t cx = (hx.y < hl.y ? 2u : 0u) | (hx.z < hl.z ? 4u : 0u) | (2u << 3);
-      const uint32_t cy = (hy.x > hl.x ? 1u : 0u) | (hy.z < hl.z ? 4u : 0u) | (3u << 3);
+      const uint32_t cz = (hz.x > hl.x ? 1u : 0u) | (hz.y < hl.y ? 2u : 0u) | (1u << 3) |
+                          (hz.x == hl.x ? 1u << 5 : (hz.y == hl.y ? 2u << 5 : 4u << 5));
+      const uint32_t cx = (hx.y < hl.y ? 2u : 0u) | (hx.z < hl.z ? 4u : 0u) | (2u << 3) | (1u << 5);
+      const uint32_t cy = (hy.x > hl.x ? 1u : 0u) | (hy.z < hl.z ? 4u : 0u) | (3u << 3) |
+                          (hy.x == hl.x ? 1u << 5 : 2u << 5);
       t[1] = vz ? hz.w : (vx ? hx.w : (vy ? hy.w : kInf));
       c[1] = vz ? cz : (vx ? cx : (vy ? cy : 0u));
       const bool s2x = vz & vx, s2y = !s2x & (vz | vx) & vy;
@@ -257,18 +270,8 @@ struct Walker {
     for (int i = 0; i < 4; ++i) {
       if (i < hc) {
         int oct = c[i] & 7;
-        const uint32_t src = c[i] >> 3;
-        if (oct == pre) {
-          // pair fix-up for a point on a bisecting plane (:301-309); rare,
-          // so the equality tests are made only here
-          float4 a = src == 0 ? e : (src == 1 ? hz : (src == 2 ? hx : hy));
-          if (a.x == hl.x)
-            oct ^= 1;
-          else if (a.y == hl.y)
-            oct ^= 2;
-          else if (a.z == hl.z)
-            oct ^= 4;
-        }
+        const uint32_t src = (c[i] >> 3) & 3u;
+        if (oct == pre) oct ^= (int)(c[i] >> 5);  // pair fix-up
         pre = oct;
         if ((occ >> oct) & 1u) {
           pk |= (uint32_t)(oct | (src << 3)) << (5 * len);
