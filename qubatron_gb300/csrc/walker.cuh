@@ -350,20 +350,45 @@ struct Walker {
     float4 isp;
     int32_t cs, cd = 0;
     int cc;
-    if (len > 0) {
+    if constexpr (EXACT && !DYN) {
+      // ---- descend (:334-367) or pop (:368-375), as one sequence ----
+      // A descent is a pop of no levels whose list and parent node are the
+      // current ones; the lanes of a warp then follow one path. A pop jumps
+      // to the nearest level above with unused candidates.
+      const bool pop = len == 0;
+      const uint32_t m = PROP ? (more & ~((1u << tdepth) - 1u)) : more;
+      if (pop && m == 0u) return kMiss;
+      const int lv = pop ? 31 - __clz(m) : level;
+      const int up = level - lv;
+      X >>= up;
+      Y >>= up;
+      Z >>= up;
+      level = lv;
+      const uint32_t saved = slot(st, level, 0);
+      const int32_t parent = pop ? (int32_t)slot(st, level, 1) : ns;
+      pk = pop ? saved : pk;
+      nx = pop ? list_next(pk) : nx;
+      if (pop) cube = cube_of_path(bc);
+      cc = list_entry(pk, nx);
+      isp = e;
+      if (pop && (cc >> 3) == 0) {
+        float4 rc, re;
+        replay_to(st, level, bc, rc, re);
+        cube = rc;
+        isp = re;
+      }
+      // the child is read again (an L1 hit) rather than kept from the
+      // node's block: 6 blocks per SM fit in the registers
+      cs = load_child(sc.tree[0], parent, level, cc & 7, oob);
+      slot(st, level, 1) = (uint32_t)parent;
+    } else if (len > 0) {
       // ---- descend into the nearest candidate (:334-367) ----
       // (a plane hit is recomputed below from its source, with the same
       // operations: cheaper than keeping all three live through the filter)
       cc = PROP ? list_entry(pk, nx) : (int)(pk & 31);
       isp = e;
-      if (DYN) {
-        cs = pick8(s0, s1, cc & 7);
-        cd = pick8(d0, d1, cc & 7);
-      } else {
-        // the static-tree kernels read the child again (an L1 hit) rather
-        // than keep the block's 8 registers live: 6 blocks per SM fit
-        cs = load_child(sc.tree[0], ns, level, cc & 7, oob);
-      }
+      cs = pick8(s0, s1, cc & 7);
+      if (DYN) cd = pick8(d0, d1, cc & 7);
       slot(st, level, 1) = (uint32_t)ns;
       if (DYN) slot(st, level, 2) = (uint32_t)nd;
     } else {
