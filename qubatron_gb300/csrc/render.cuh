@@ -479,14 +479,17 @@ constexpr int kServiceMinDefault = 4;
 // PROP), shading and flare.
 // Minimum resident blocks per SM the register allocation must allow: the
 // walk is latency-bound per warp, so more resident warps pay as long as
-// nothing spills (static tree: 6, 80 registers; both trees: 5, 96).
-template <bool DYN, int MODE>
+// nothing (or next to nothing) spills: 6 (80 registers) for the fused and
+// primary-pass kernels; the shade passes, which also shade and test
+// proposals, and the two-tree walk of an inexact basecube (which keeps the
+// node blocks live) keep 5 with both trees and no bound with one.
+template <bool EXACT, bool DYN, int MODE>
 constexpr int render_min_blocks() {
-  return DYN ? 5 : (MODE == kShadePass ? 1 : 6);
+  return (MODE == kShadePass || (DYN && !EXACT)) ? (DYN ? 5 : 1) : 6;
 }
 
 template <bool EXACT, bool DYN, int MODE, bool PROP>
-__global__ void __launch_bounds__(kThreads, render_min_blocks<DYN, MODE>()) render_kernel(DevScene sc, const __grid_constant__ Batch batch,
+__global__ void __launch_bounds__(kThreads, render_min_blocks<EXACT, DYN, MODE>()) render_kernel(DevScene sc, const __grid_constant__ Batch batch,
                                                           unsigned int* queue, const __grid_constant__ Wave wave) {
   extern __shared__ uint32_t smem[];
   const int tid = threadIdx.x, lane = tid & 31;

@@ -350,7 +350,7 @@ struct Walker {
     float4 isp;
     int32_t cs, cd = 0;
     int cc;
-    if constexpr (EXACT && !DYN) {
+    if constexpr (EXACT) {
       // ---- descend (:334-367) or pop (:368-375), as one sequence ----
       // A descent is a pop of no levels whose list and parent node are the
       // current ones; the lanes of a warp then follow one path. A pop jumps
@@ -366,6 +366,8 @@ struct Walker {
       level = lv;
       const uint32_t saved = slot(st, level, 0);
       const int32_t parent = pop ? (int32_t)slot(st, level, 1) : ns;
+      int32_t parent_d = 0;
+      if (DYN) parent_d = pop ? (int32_t)slot(st, level, 2) : nd;
       pk = pop ? saved : pk;
       nx = pop ? list_next(pk) : nx;
       if (pop) cube = cube_of_path(bc);
@@ -381,6 +383,10 @@ struct Walker {
       // node's block: 6 blocks per SM fit in the registers
       cs = load_child(sc.tree[0], parent, level, cc & 7, oob);
       slot(st, level, 1) = (uint32_t)parent;
+      if (DYN) {
+        cd = load_child(sc.tree[1], parent_d, level, cc & 7, oob);
+        slot(st, level, 2) = (uint32_t)parent_d;
+      }
     } else if (len > 0) {
       // ---- descend into the nearest candidate (:334-367) ----
       // (a plane hit is recomputed below from its source, with the same
