@@ -162,27 +162,42 @@ struct Walker {
 
     // ---- subnode test (octree_fsh.c:251-329) ----
     int4 s0, s1, d0, d1;
-    if (load_block(sc.tree[0], ns, level, s0, s1, oob)) ++vis_s;
+    // with one tree a node below the root is always a child index > 0 (the
+    // walk only enters occupied children), so the node-0 rule needs no test
+    if (load_block(sc.tree[0], ns, DYN ? level : 0, s0, s1, oob)) ++vis_s;
     if (DYN) {
       if (load_block(sc.tree[1], nd, level, d0, d1, oob)) ++vis_d;
     }
     float4 cb = brb_of(cube);
     float3 hl = hlf_of(cube);
     // a ray parallel to a bisecting plane has no hit on it (the shader's
-    // FLT_MAX sentinel fails the face test)
+    // FLT_MAX sentinel fails the face test). With the reciprocal the
+    // parallel component's reciprocal is 0, so the hit's t is +-0 and fails
+    // t > 0 by itself; the single-tree kernels skip the test there (the
+    // two-tree ones keep one form, which needs fewer registers).
     float4 hz, hx, hy;
-    if (EXACT && fast) {
+    bool vz, vx, vy;
+    if (EXACT && !DYN && fast) {
       hz = hit_zplane_rcp(hl.z, p, d, inv.z);
       hx = hit_xplane_rcp(hl.x, p, d, inv.x);
       hy = hit_yplane_rcp(hl.y, p, d, inv.y);
+      vz = (hz.w > 0.0f) & in_zface(hz, cube, cb);
+      vx = (hx.w > 0.0f) & in_xface(hx, cube, cb);
+      vy = (hy.w > 0.0f) & in_yface(hy, cube, cb);
     } else {
-      hz = hit_zplane_raw(hl.z, p, d);
-      hx = hit_xplane_raw(hl.x, p, d);
-      hy = hit_yplane_raw(hl.y, p, d);
+      if (EXACT && fast) {
+        hz = hit_zplane_rcp(hl.z, p, d, inv.z);
+        hx = hit_xplane_rcp(hl.x, p, d, inv.x);
+        hy = hit_yplane_rcp(hl.y, p, d, inv.y);
+      } else {
+        hz = hit_zplane_raw(hl.z, p, d);
+        hx = hit_xplane_raw(hl.x, p, d);
+        hy = hit_yplane_raw(hl.y, p, d);
+      }
+      vz = (d.z != 0.0f) & (hz.w > 0.0f) & in_zface(hz, cube, cb);
+      vx = (d.x != 0.0f) & (hx.w > 0.0f) & in_xface(hx, cube, cb);
+      vy = (d.y != 0.0f) & (hy.w > 0.0f) & in_yface(hy, cube, cb);
     }
-    bool vz = (d.z != 0.0f) & (hz.w > 0.0f) & in_zface(hz, cube, cb);
-    bool vx = (d.x != 0.0f) & (hx.w > 0.0f) & in_xface(hx, cube, cb);
-    bool vy = (d.y != 0.0f) & (hy.w > 0.0f) & in_yface(hy, cube, cb);
 
     // Candidates in the shader's fill order (entry, z, x, y), compacted, as
     // (t, code): code = octet side bits | source << 3 | flip << 5. A
@@ -380,8 +395,13 @@ struct Walker {
         isp = re;
       }
       // the child is read again (an L1 hit) rather than kept from the
-      // node's block: 6 blocks per SM fit in the registers
-      cs = load_child(sc.tree[0], parent, level, cc & 7, oob);
+      // node's block: 6 blocks per SM fit in the registers. With one tree
+      // the parent is a node whose block was read (a candidate exists only
+      // below an occupied octet), so the index needs no checks.
+      if (DYN)
+        cs = load_child(sc.tree[0], parent, level, cc & 7, oob);
+      else
+        cs = __ldg(reinterpret_cast<const int32_t*>(sc.tree[0].child) + 8 * (uint32_t)parent + (cc & 7));
       slot(st, level, 1) = (uint32_t)parent;
       if (DYN) {
         cd = load_child(sc.tree[1], parent_d, level, cc & 7, oob);
