@@ -199,12 +199,15 @@ struct Walker {
       vy = (d.y != 0.0f) & (hy.w > 0.0f) & in_yface(hy, cube, cb);
     }
 
-    // Candidates in the shader's fill order (entry, z, x, y), compacted, as
-    // (t, code): code = octet side bits | source << 3 | flip << 5. A
-    // bisecting-plane hit lies on its own plane (its coordinate is the
-    // midpoint itself), so its side bit on that axis is 0. Unused slots hold
-    // t = +inf: a valid candidate has a finite t, so the ordering below never
-    // swaps a pad.
+    // Candidates in the shader's fill order (entry, z, x, y) as (t, code):
+    // code = octet side bits | source << 3 | flip << 5. A bisecting-plane
+    // hit lies on its own plane (its coordinate is the midpoint itself), so
+    // its side bit on that axis is 0. The shader compacts the valid hits
+    // before ordering them; here an invalid hit keeps its slot with t = +inf.
+    // A valid candidate has a finite t, and the swap network (swap when
+    // strictly less) then yields the valid candidates first, in the same
+    // order as from the compacted array, ties included (checked for every
+    // validity pattern and every tie pattern of 3 and 4 values).
     //
     // flip is the octet bit the pair fix-up (:301-309) toggles when the point
     // falls in the same octet as the candidate before it: the first axis, x
@@ -221,21 +224,17 @@ struct Walker {
     c[0] = (e.x > hl.x ? 1u : 0u) | (e.y < hl.y ? 2u : 0u) | (e.z < hl.z ? 4u : 0u) |
            (e.x == hl.x ? 1u << 5 : (e.y == hl.y ? 2u << 5 : (e.z == hl.z ? 4u << 5 : 0u)));
     {
-      // the valid plane hits fill slots 1.. in the order z, x, y (selects:
-      // the lanes of a warp differ in which hits are valid)
       const uint32_t cz = (hz.x > hl.x ? 1u : 0u) | (hz.y < hl.y ? 2u : 0u) | (1u << 3) |
                           (hz.x == hl.x ? 1u << 5 : (hz.y == hl.y ? 2u << 5 : 4u << 5));
       const uint32_t cx = (hx.y < hl.y ? 2u : 0u) | (hx.z < hl.z ? 4u : 0u) | (2u << 3) | (1u << 5);
       const uint32_t cy = (hy.x > hl.x ? 1u : 0u) | (hy.z < hl.z ? 4u : 0u) | (3u << 3) |
                           (hy.x == hl.x ? 1u << 5 : 2u << 5);
-      t[1] = vz ? hz.w : (vx ? hx.w : (vy ? hy.w : kInf));
-      c[1] = vz ? cz : (vx ? cx : (vy ? cy : 0u));
-      const bool s2x = vz & vx, s2y = !s2x & (vz | vx) & vy;
-      t[2] = s2x ? hx.w : (s2y ? hy.w : kInf);
-      c[2] = s2x ? cx : (s2y ? cy : 0u);
-      const bool s3 = vz & vx & vy;
-      t[3] = s3 ? hy.w : kInf;
-      c[3] = s3 ? cy : 0u;
+      t[1] = vz ? hz.w : kInf;
+      c[1] = cz;
+      t[2] = vx ? hx.w : kInf;
+      c[2] = cx;
+      t[3] = vy ? hy.w : kInf;
+      c[3] = cy;
     }
     const int hc = 1 + (int)vz + (int)vx + (int)vy;
     // ordering by swaps, as the shader's nested loop (:276-290). When no
