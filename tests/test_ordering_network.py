@@ -44,4 +44,4 @@ def test_three_slot_network_in_place_equals_compacted():
 
 
 def test_four_slot_network_in_place_equals_compacted():
-    assert _check(3, with_entry=True) == 8 * 5 ** 4
+    assert _check(3, with_entry=True) == 8 * 4 ** 4
