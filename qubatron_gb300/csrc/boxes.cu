@@ -43,21 +43,52 @@ int grid_of(int64_t n) {
   return (int)(b < 1 ? 1 : (b > 4096 ? 4096 : b));
 }
 
-// Children of the nodes in [in_b, in_e) of `order` appended after out_b.
+// Children of the nodes in [in_b, in_e) of `order` appended at the end of
+// the order (the counter). One counter update per warp and pass: each lane
+// takes its node's children, the warp reserves their total at once.
 __global__ void expand_kernel(const int32_t* __restrict__ child, int64_t n, int32_t* __restrict__ order,
                               int64_t in_b, int64_t in_e, unsigned long long* __restrict__ count) {
-  for (int64_t j = in_b + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < in_e;
-       j += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t node = order[j];
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  // the loop's trip count is the same for the whole warp (ballots below)
+  for (int64_t j0 = in_b + (blockIdx.x * (int64_t)blockDim.x + threadIdx.x - lane); j0 < in_e; j0 += stride) {
+    const int64_t j = j0 + lane;
+    int32_t c[8];
+    uint32_t take = 0;
+    bool outside = false;
+    if (j < in_e) {
+      const int32_t node = order[j];
+      const int4* p = reinterpret_cast<const int4*>(child + (int64_t)node * 8);
+      const int4 a = p[0], b = p[1];
+      c[0] = a.x; c[1] = a.y; c[2] = a.z; c[3] = a.w;
+      c[4] = b.x; c[5] = b.y; c[6] = b.z; c[7] = b.w;
+#pragma unroll
+      for (int o = 0; o < 8; ++o) {
+        take |= (c[o] > 0 && c[o] < n) ? (1u << o) : 0u;
+        // an index outside the array: the walk must meet it (it reports
+        // it), so no boxes for this tree
+        outside |= c[o] != 0 && !(c[o] > 0 && c[o] < n);
+      }
+    }
+    const unsigned mine = (unsigned)__popc(take);
+    unsigned incl = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const unsigned total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    const bool any_outside = __any_sync(0xFFFFFFFFu, outside);
+    unsigned long long base = 0;
+    if (lane == 31 && (total || any_outside))
+      base = atomicAdd(count, (unsigned long long)total + (any_outside ? (unsigned long long)n + 1ull : 0ull));
+    base = __shfl_sync(0xFFFFFFFFu, base, 31);
+    unsigned long long k = base + (incl - mine);
+#pragma unroll
     for (int o = 0; o < 8; ++o) {
-      const int32_t c = child[(int64_t)node * 8 + o];
-      if (c > 0 && c < n) {
-        const unsigned long long k = atomicAdd(count, 1ull);
-        if ((int64_t)k < n) order[k] = c;  // past n: not a tree, detected on the host
-      } else if (c != 0) {
-        // an index outside the array: the walk must meet it (it reports it),
-        // so no boxes for this tree
-        atomicAdd(count, (unsigned long long)n + 1ull);
+      if ((take >> o) & 1u) {
+        if ((int64_t)k < n) order[k] = c[o];  // past n: not a tree, detected on the host
+        ++k;
       }
     }
   }
