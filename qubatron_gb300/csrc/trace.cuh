@@ -296,7 +296,8 @@ __device__ __forceinline__ uint2 child_box_word(const uint32_t* rec, int o) {
 // of a child's edge) into the cube (u; y and z count downward). A bound q
 // units into the cube is then one FMA: a + q * u. Against the direct slab
 // test this regroups (c + q * unit +- m - p) / d; the extra rounding is a
-// few ulps of coordinates below 9 S, about 2^-20 S, far inside m = 2^-14 S.
+// few ulps of coordinates below 9 S (one ulp is at most 2^-19 S), far inside
+// m = 2^-14 S.
 struct BoxFrame {
   float a0[3], a1[3], u[3];
 };
