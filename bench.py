@@ -256,7 +256,9 @@ def run_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
         "config": {"workload": WORKLOAD, "points": scene.points.shape[0], "nodes": int(scene.nodes.shape[0]),
                    "resolution": f"{w.width}x{w.height}", "views": len(views), "depth": 12, "basecube": 1800.0},
-        "cpu_baseline": {k: res[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": res["cores"], "kind": res["kind"],
+                         "sample": f"{args.steps} timed steps, {rays_total} rays in {sum(times):.1f} s; each step "
+                                   f"a seeded pixel sample of the workload (last: {res['sample']})"},
         "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference's own path is a GLSL fragment shader (no graphics stack here); this is its C "
                 "restatement (oracle/) on all host cores, per step a seeded pixel sample of the workload",
