@@ -216,6 +216,12 @@ WORKLOADS = {
 _b64_sizes, _b64_poses = batch_views(64, 64)
 WORKLOADS["floor1m_char2m_mixed_x64"] = Workload("floor1m_char2m_mixed_x64", "floor1m", 0, 0, _b64_poses,
                                                  sizes=_b64_sizes, character=2_000_000)
+# one 1920x1080 view of the same floor and 2M-point character (camera on the
+# ring, aimed at the character): a small case of the two-tree kernel for
+# profiling
+WORKLOADS["floor1m_char2m_1920x1080x1"] = Workload("floor1m_char2m_1920x1080x1", "floor1m", 1920, 1080,
+                                                   batch_views(65, 1, target=(900.0, 500.0, 1100.0))[1],
+                                                   character=2_000_000)
 # learned occluder proposal on the floor scene: 256 training poses at 960x720
 # (about 10^7 logged shadow rays), 16 held-out poses at 1920x1080
 WORKLOADS["floor1m_mlp_1920x1080x16"] = Workload("floor1m_mlp_1920x1080x16", "floor1m", 1920, 1080,
