@@ -31,11 +31,16 @@ extern "C" {
 #endif
 
 /* One tree in the reference layout: 12 int32 per node (8 children, model
- * index, 3 pad), node 0 = root, child index 0 = empty (octree.c:11-14). */
+ * index, 3 pad), node 0 = root, child index 0 = empty (octree.c:11-14).
+ * cbox / box_depth: leaf-box records of qbo_build_boxes (16 words per node)
+ * and the depth they were built for; NULL (the default) walks as the shader,
+ * with no pruning. */
 typedef struct qbo_tree
 {
-    const int32_t* nodes;
-    int64_t        n_nodes;
+    const int32_t*  nodes;
+    int64_t         n_nodes;
+    const uint32_t* cbox;
+    int32_t         box_depth;
 } qbo_tree;
 
 /* Per-point float3 attribute arrays (model.c:14-25). */
@@ -136,6 +141,20 @@ void qbo_render_pixels(const qbo_scene* sc, const qbo_view* v, const int32_t* px
  * frame-constant parts of main() (octree_fsh.c:403-418). focal <= 0 selects
  * the reference focal length (dim.x/2)/tan(PI/4). */
 void qbo_view_setup(float width, float height, const float position[3], const float angle[3], float lighta, int quality, int maxlevel, float basesize, int shoot, float focal, qbo_view* out);
+
+/* Leaf-box pruning of the CUDA library (no reference counterpart), restated
+ * to check the pruned walk's visit counts; see qbo_boxes.c.
+ * qbo_build_boxes fills rec (16 words per node) and returns the tree's depth,
+ * or -1 when the array is not usable (a node reached twice, a child index
+ * outside the array, deeper than 17 levels). */
+typedef struct qbo_box_frame_t
+{
+    float a0[3], a1[3], u[3];
+} qbo_box_frame_t;
+int32_t qbo_build_boxes(const int32_t* nodes, int64_t n, uint32_t* rec);
+void    qbo_box_frame(const float cube[4], const float p[3], const float inv[3], float m, qbo_box_frame_t* f);
+int     qbo_box_hit(uint32_t rx, uint32_t ry, int o, const qbo_box_frame_t* f);
+int     qbo_box_ray_ok(const float bc[4], int maxlevel, const float p[3], const float d[3]);
 
 /* GL float -> unorm8 conversion used for the RGBA8 target (octree_glc.c:237). */
 uint8_t qbo_unorm8(float f);

@@ -26,7 +26,7 @@ i64p = C.POINTER(C.c_int64)
 
 
 class QboTree(C.Structure):
-    _fields_ = [("nodes", i32p), ("n_nodes", C.c_int64)]
+    _fields_ = [("nodes", i32p), ("n_nodes", C.c_int64), ("cbox", u32p), ("box_depth", C.c_int32)]
 
 
 class QboModel(C.Structure):
@@ -116,6 +116,8 @@ def qbo() -> C.CDLL:
         lib.qbo_remove_point.argtypes = [i32p, C.c_float, C.c_int, f32p, i32p, i32p]
         lib.qbo_remove_point.restype = None
         lib.qbo_point_octets.argtypes = [C.c_float, C.c_int, f32p, i32p]
+        lib.qbo_build_boxes.argtypes = [i32p, C.c_int64, u32p]
+        lib.qbo_build_boxes.restype = C.c_int32
         lib.qbo_point_octets.restype = None
         _qbo = lib
     return _qbo
@@ -152,9 +154,11 @@ def _p(a: np.ndarray, t):
 
 
 class Scene:
-    """Arrays of one scene kept alive for the oracle (static [+ dynamic])."""
+    """Arrays of one scene kept alive for the oracle (static [+ dynamic]).
+    boxes=True adds the CUDA library's leaf-box records (qbo_build_boxes), so
+    the walk prunes as the library does; the default walks as the shader."""
 
-    def __init__(self, s_nodes, s_col, s_nrm, d_nodes=None, d_col=None, d_nrm=None):
+    def __init__(self, s_nodes, s_col, s_nrm, d_nodes=None, d_col=None, d_nrm=None, boxes=False):
         c32 = lambda a, dt: None if a is None else np.ascontiguousarray(a, dtype=dt)  # noqa: E731
         self.arrays = [c32(s_nodes, np.int32), c32(s_col, np.float32), c32(s_nrm, np.float32),
                        c32(d_nodes, np.int32), c32(d_col, np.float32), c32(d_nrm, np.float32)]
@@ -169,6 +173,21 @@ class Scene:
             if col is not None and nrm is not None:
                 npts = min(col.size // 3, nrm.size // 3)
             sc.model[t].n_points = npts
+        self.box_depth = [-1, -1]
+        if boxes:
+            lib = qbo()
+            for t in range(2):
+                nodes = self.arrays[3 * t]
+                if nodes is None or nodes.size == 0:
+                    continue
+                n = nodes.size // 12
+                rec = np.zeros(n * 16, np.uint32)
+                depth = lib.qbo_build_boxes(_p(nodes, i32p), n, _p(rec, u32p))
+                self.box_depth[t] = depth
+                if depth >= 0:
+                    self.arrays.append(rec)
+                    sc.tree[t].cbox = _p(rec, u32p)
+                    sc.tree[t].box_depth = depth
         self.c = sc
 
 

@@ -184,6 +184,17 @@ void qbo_trace(const qbo_scene* sc, const float bc[4], int maxlevel, const float
     const qbo_tree* td = &sc->tree[1];
     int64_t         pushes = 0;
 
+    /* leaf-box pruning of the CUDA library, when the scene carries boxes
+     * (qbo_boxes.c; off by default): the ray conditions, the reciprocal
+     * direction and the margin 2^-14 S */
+    const int box_ray = (ts->cbox || td->cbox) && qbo_box_ray_ok(bc, maxlevel, pos, dir);
+    const int box_s   = box_ray && ts->cbox && maxlevel >= ts->box_depth;
+    const int box_d   = box_ray && td->cbox && td->n_nodes > 0 && maxlevel >= td->box_depth;
+    float     inv[3]  = {0.0f, 0.0f, 0.0f};
+    if (box_ray)
+        for (int k = 0; k < 3; ++k) inv[k] = 1.0f / dir[k];
+    const float box_m = bc[3] * 6.1035156e-05f;
+
     for (;;)
     {
         out->steps++;
@@ -240,6 +251,16 @@ void qbo_trace(const qbo_scene* sc, const float bc[4], int maxlevel, const float
             hitc    = 1;
             hitp[0] = L->isps[0];
 
+            /* pruning: a level whose children are not all leaf cells */
+            const int lev_s = box_s && level + 1 < ts->box_depth;
+            const int lev_d = box_d && level + 1 < td->box_depth;
+            qbo_box_frame_t bf;
+            if (lev_s || lev_d)
+            {
+                const float cube4[4] = {tlf.x, tlf.y, tlf.z, tlf.w};
+                qbo_box_frame(cube4, pos, inv, box_m, &bf);
+            }
+
             act = hit_zplane(hlf.z, pos, dir);
             if (act.w > 0.0f && in_zface(act, tlf, cb)) hitp[hitc++] = act;
             act = hit_xplane(hlf.x, pos, dir);
@@ -282,7 +303,18 @@ void qbo_trace(const qbo_scene* sc, const float bc[4], int maxlevel, const float
 
                 int32_t cs = node_slot(ts, L->node[0], oct, level, &out->oob);
                 int32_t cd = node_slot(td, L->node[1], oct, level, &out->oob);
-                if (cs > 0 || cd > 0)
+                int     keep = cs > 0 || cd > 0;
+                if (keep && (lev_s || lev_d))
+                {
+                    /* a child is kept while a tree holding it may have a
+                     * leaf near the ray */
+                    const uint32_t* rs = lev_s ? ts->cbox + (int64_t) L->node[0] * 16 : NULL;
+                    const uint32_t* rd = lev_d ? td->cbox + (int64_t) L->node[1] * 16 : NULL;
+                    const int hs = cs > 0 && (!rs || qbo_box_hit(rs[2 * oct], rs[2 * oct + 1], oct, &bf));
+                    const int hd = cd > 0 && (!rd || qbo_box_hit(rd[2 * oct], rd[2 * oct + 1], oct, &bf));
+                    keep = hs || hd;
+                }
+                if (keep)
                 {
                     int len      = L->ispsi & 0x0F;
                     L->octs[len] = oct;

@@ -18,9 +18,10 @@
 // Levels: the build walks the tree breadth first from the root; the depth of
 // the tree is the last level that holds nodes, and the boxes are valid for
 // renders whose maxlevel is at least that depth. A node reached twice (not a
-// tree), a child index outside the array (which the walk reports when it
-// meets it) or a tree deeper than the shader's stack leaves the boxes
-// unusable.
+// tree: two parents or a cycle, found from each node's position in the
+// breadth-first order), a child index outside the array (which the walk
+// reports when it meets it) or a tree deeper than the shader's stack leaves
+// the boxes unusable.
 
 #include <cuda_runtime.h>
 #include <thrust/device_vector.h>
@@ -44,10 +45,12 @@ int grid_of(int64_t n) {
 }
 
 // Children of the nodes in [in_b, in_e) of `order` appended at the end of
-// the order (the counter). One counter update per warp and pass: each lane
-// takes its node's children, the warp reserves their total at once.
+// the order (the counter), each with its position in pos. One counter update
+// per warp and pass: each lane takes its node's children, the warp reserves
+// their total at once.
 __global__ void expand_kernel(const int32_t* __restrict__ child, int64_t n, int32_t* __restrict__ order,
-                              int64_t in_b, int64_t in_e, unsigned long long* __restrict__ count) {
+                              int32_t* __restrict__ pos, int64_t in_b, int64_t in_e,
+                              unsigned long long* __restrict__ count) {
   const int lane = threadIdx.x & 31;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   // the loop's trip count is the same for the whole warp (ballots below)
@@ -87,11 +90,22 @@ __global__ void expand_kernel(const int32_t* __restrict__ child, int64_t n, int3
 #pragma unroll
     for (int o = 0; o < 8; ++o) {
       if ((take >> o) & 1u) {
-        if ((int64_t)k < n) order[k] = c[o];  // past n: not a tree, detected on the host
+        if ((int64_t)k < n) {  // past n: not a tree, detected on the host
+          order[k] = c[o];
+          pos[c[o]] = (int32_t)k;
+        }
         ++k;
       }
     }
   }
+}
+
+// A node appended twice (two parents, or a cycle) keeps one of its positions
+// in pos, so another position of it disagrees: then the array is not a tree.
+__global__ void unique_kernel(const int32_t* __restrict__ order, const int32_t* __restrict__ pos, int64_t total,
+                              unsigned int* __restrict__ dup) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < total; j += (int64_t)gridDim.x * blockDim.x)
+    if (pos[order[j]] != (int32_t)j) *dup = 1u;
 }
 
 // Exact boxes in leaf cells relative to each node's cube, for the nodes of one
@@ -163,10 +177,14 @@ int build_child_boxes(const int32_t* child, int64_t n, uint32_t* rec, cudaStream
   *depth = -1;
   if (n <= 0) return QBC_OK;
   try {
-    thrust::device_vector<int32_t> order(n);
+    thrust::device_vector<int32_t> order(n), pos(n);
     thrust::device_vector<unsigned long long> count(1);
+    thrust::device_vector<unsigned int> dup(1);
     int32_t zero = 0;
+    unsigned int no = 0u;
     cudaMemcpyAsync(thrust::raw_pointer_cast(order.data()), &zero, 4, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(thrust::raw_pointer_cast(pos.data()), &zero, 4, cudaMemcpyHostToDevice, stream);
+    cudaMemcpyAsync(thrust::raw_pointer_cast(dup.data()), &no, 4, cudaMemcpyHostToDevice, stream);
     // breadth first: level L holds order[off[L], off[L+1])
     std::vector<int64_t> off = {0, 1};
     unsigned long long total = 1;
@@ -174,7 +192,8 @@ int build_child_boxes(const int32_t* child, int64_t n, uint32_t* rec, cudaStream
     for (int L = 0; L <= kMaxDepth; ++L) {
       const int64_t b = off[L], e = off[L + 1];
       if (e == b) break;
-      expand_kernel<<<grid_of(e - b), 256, 0, stream>>>(child, n, thrust::raw_pointer_cast(order.data()), b, e,
+      expand_kernel<<<grid_of(e - b), 256, 0, stream>>>(child, n, thrust::raw_pointer_cast(order.data()),
+                                                         thrust::raw_pointer_cast(pos.data()), b, e,
                                                          thrust::raw_pointer_cast(count.data()));
       ++*launches;
       cudaError_t err = cudaMemcpyAsync(&total, thrust::raw_pointer_cast(count.data()), 8, cudaMemcpyDeviceToHost,
@@ -183,6 +202,19 @@ int build_child_boxes(const int32_t* child, int64_t n, uint32_t* rec, cudaStream
       if (err != cudaSuccess) return fail(QBC_E_CUDA, "box build: %s", cudaGetErrorString(err));
       if ((int64_t)total > n) return QBC_OK;  // a node reached twice: no boxes
       off.push_back((int64_t)total);
+    }
+    // every node once (the counter alone misses a node reached twice when
+    // others are unreachable)
+    {
+      unique_kernel<<<grid_of(off.back()), 256, 0, stream>>>(thrust::raw_pointer_cast(order.data()),
+                                                            thrust::raw_pointer_cast(pos.data()), off.back(),
+                                                            thrust::raw_pointer_cast(dup.data()));
+      ++*launches;
+      unsigned int d = 0u;
+      cudaError_t err = cudaMemcpyAsync(&d, thrust::raw_pointer_cast(dup.data()), 4, cudaMemcpyDeviceToHost, stream);
+      if (err == cudaSuccess) err = cudaStreamSynchronize(stream);
+      if (err != cudaSuccess) return fail(QBC_E_CUDA, "box build: %s", cudaGetErrorString(err));
+      if (d) return QBC_OK;  // a node reached twice: no boxes
     }
     // the deepest level with nodes
     int D = 0;

@@ -13,8 +13,8 @@ def upload_scene(ctx, s_nodes, s_col, s_nrm, d_nodes=None, d_col=None, d_nrm=Non
         ctx.upload_octree(True, d_nodes)
 
 
-def oracle_scene(qbo, s_nodes, s_col, s_nrm, d_nodes=None, d_col=None, d_nrm=None):
-    return qbo.Scene(s_nodes, s_col, s_nrm, d_nodes, d_col, d_nrm)
+def oracle_scene(qbo, s_nodes, s_col, s_nrm, d_nodes=None, d_col=None, d_nrm=None, boxes=False):
+    return qbo.Scene(s_nodes, s_col, s_nrm, d_nodes, d_col, d_nrm, boxes=boxes)
 
 
 def bits(a: np.ndarray) -> np.ndarray:
@@ -23,8 +23,9 @@ def bits(a: np.ndarray) -> np.ndarray:
 
 def compare_frame(gpu: dict, ref: dict, where: str = "", visits: bool = False) -> dict:
     """Bit-exact comparison of every stream; returns counts for reporting.
-    The per-pixel visit counts match the oracle's only with box pruning off
-    (QBC_OPT_BOX_PRUNE 0); visits=True compares them too."""
+    The per-pixel visit counts match the oracle's when both walk alike: box
+    pruning off (QBC_OPT_BOX_PRUNE 0) against the plain oracle, or on against
+    an oracle scene with boxes; visits=True compares them too."""
     key = {"rgba32f": "rgba"}
     for s in STREAMS:
         if s == "visits" and not visits:

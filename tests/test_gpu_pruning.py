@@ -175,3 +175,59 @@ def test_box_word_counter(ctx, floor50k_scene):
     visits = sum(int(b["visits"].astype(np.int64).sum()) for b in bufs)
     assert 0 < st["box_words"] <= 8 * visits, (st["box_words"], visits)
     assert st["shadow_rays"] > 0
+
+
+def test_pruned_walk_matches_the_oracle_with_boxes(ctx, oracle, floor50k_scene):
+    """With pruning on, every stream, the visit counts included, equals the
+    oracle's walk with the restated filter (oracle/qbo_boxes.c): one tree and
+    two trees, fused and two-pass frames, and ray queries."""
+    import qubatron_gb300._lib as L
+    from qubatron_gb300 import build_octree, scenes
+    from test_gpu_parity import _ray_parity
+    s = floor50k_scene
+    ctx.set_option(L.OPT_BOX_PRUNE, 1)
+    upload_scene(ctx, s.nodes, s.colors, s.normals)
+    sc = oracle_scene(oracle, s.nodes, s.colors, s.normals, boxes=True)
+    assert sc.box_depth[0] == LEVELS
+    for v in _views():
+        compare_frame(gpu_frame(ctx, v), oracle.render(sc, oracle.QboView.from_bytes(v.to_bytes())), "one tree",
+                      visits=True)
+    rng = np.random.default_rng(7)
+    pos = rng.uniform(0, S, (3000, 3)).astype(np.float32)
+    dirs = rng.normal(size=(3000, 3)).astype(np.float32)
+    _ray_parity(ctx, oracle, sc, pos, dirs, visits=True)
+    ch = scenes.make_character(40_000, root=(800.0, 60.0, 1100.0))
+    p, n = scenes.skin_reference(ch, scenes.pose_bones(ch, 1))
+    dn = build_octree(p)
+    upload_scene(ctx, s.nodes, s.colors, s.normals, dn, ch.colors, n)
+    sc = oracle_scene(oracle, s.nodes, s.colors, s.normals, dn, ch.colors, n, boxes=True)
+    views = _views(shoot=1)
+    ref = [oracle.render(sc, oracle.QboView.from_bytes(v.to_bytes())) for v in views]
+    for v, r in zip(views, ref):
+        compare_frame(gpu_frame(ctx, v), r, "two trees", visits=True)
+    got, _ = ctx.render_host_ex(views, STREAMS, two_pass=True)
+    for g, r in zip(got, ref):
+        compare_frame(g.arrays, r, "two trees, two-pass", visits=True)
+
+
+def test_boxes_refused_when_a_node_has_two_parents(ctx):
+    """A node below two parents at different levels would get a box for one
+    of them only: the library builds no boxes for such an array, also when
+    the breadth-first walk appends no more nodes than the array holds."""
+    import qubatron_gb300._lib as L
+    nodes = np.zeros((40, 12), np.int32)  # nodes 17.. unreachable
+    for o in range(8):
+        nodes[0, o] = 1 + o
+        nodes[1 + o, 0] = 9 + o
+    col = np.ones((1, 3), np.float32)
+    nrm = np.tile([0.0, 0.0, -1.0], (1, 1)).astype(np.float32)
+    ctx.set_option(L.OPT_BOX_PRUNE, 1)
+    views = _views(maxlevel=2)
+    upload_scene(ctx, nodes, col, nrm)
+    _, st = ctx.render_host_ex(views, ("rgba8", "visits"))
+    assert st["box_words"] > 0  # a tree: boxes built and read
+    dag = nodes.copy()
+    dag[9, 0] = 2  # node 2 (level 1) also below node 9 (level 2)
+    upload_scene(ctx, dag, col, nrm)
+    _, st = ctx.render_host_ex(views, ("rgba8", "visits"))
+    assert st["box_words"] == 0
