@@ -89,3 +89,32 @@ def test_pruned_oracle_walk_keeps_every_pixel(oracle):
             assert np.array_equal(a[k].view(np.uint8), b[k].view(np.uint8)), k
         assert (b["visits"] <= a["visits"]).all()
         assert b["visits"].sum() < 0.9 * a["visits"].sum()
+
+
+def test_pruned_two_tree_walk_keeps_every_pixel(oracle):
+    from qubatron_gb300 import scenes
+    nodes, col, nrm = _scene()
+    ch = scenes.make_character(30_000, root=(800.0, 60.0, 1100.0))
+    p, n = scenes.skin_reference(ch, scenes.pose_bones(ch, 1))
+    dn = oracle.build_tree(p, S, LEVELS)
+    plain = oracle.Scene(nodes, col, nrm, dn, ch.colors, n)
+    pruned = oracle.Scene(nodes, col, nrm, dn, ch.colors, n, boxes=True)
+    assert pruned.box_depth == [LEVELS, LEVELS]
+    v = oracle.view_setup(160, 120, (500.2, 600.9, 1500.3), (-0.4, -0.45, 0.0), 1.1, 10, LEVELS, S, 1, 0.0)
+    a, b = oracle.render(plain, v), oracle.render(pruned, v)
+    for k in ("rgba", "rgba8", "flags", "leaf", "isp"):
+        assert np.array_equal(a[k].view(np.uint8), b[k].view(np.uint8)), k
+    assert b["visits"].sum() < a["visits"].sum()
+
+
+def test_no_pruning_where_the_filter_does_not_apply(oracle):
+    """An inexact basecube, or a maxlevel below the tree's depth: the walk
+    with boxes is the shader's walk, visit counts included."""
+    nodes, col, nrm = _scene(5_000)
+    plain = oracle.Scene(nodes, col, nrm)
+    pruned = oracle.Scene(nodes, col, nrm, boxes=True)
+    for bs, ml in ((1234.567, LEVELS), (S, LEVELS - 2)):
+        v = oracle.view_setup(96, 64, (903.7, 421.3, 1702.9), (0.0, -0.3, 0.0), 0.0, 10, ml, bs, 0, 0.0)
+        a, b = oracle.render(plain, v), oracle.render(pruned, v)
+        for k in a:
+            assert np.array_equal(a[k].view(np.uint8), b[k].view(np.uint8)), (bs, ml, k)
