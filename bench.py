@@ -120,6 +120,63 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def scene_digest(scene) -> str:
+    """SHA-256 of the scene's points, normals and colours: both arms of the
+    benchmark state it, so they provably render the same scene."""
+    import hashlib
+    h = hashlib.sha256()
+    for a in (scene.points, scene.normals, scene.colors):
+        h.update(memoryview(np.ascontiguousarray(a)).cast("B"))
+    return h.hexdigest()
+
+
+def workload_config(w, scene, n_nodes: int, views) -> dict:
+    """The `config` object of both arms' JSON lines: the workload alone,
+    identical for the GPU arm and the reference arm."""
+    pixels = sum(v.width_px * v.height_px for v in views)
+    return {"workload": w.name, "points": int(scene.points.shape[0]), "nodes": int(n_nodes),
+            "scene_sha256": scene_digest(scene),
+            "resolution": f"{w.width}x{w.height}" if w.width else "mixed", "views": len(views), "pixels": pixels,
+            "depth": 12, "basecube": 1800.0, "dynamic_points": int(w.character),
+            "per_step": "re-skin + rebuild dynamic tree + render" if w.character else "render",
+            "l2": "GPU arm: flushed between steps (2x L2 write, outside the timed events); node arrays "
+                  f"{n_nodes * 36 / 1e9:.2f} GB > L2",
+            "parallelism": "replicas only" if dist_env()[1] > 1 else "single GPU"}
+
+
+def prepare_reference(workload_name: str):
+    """The workload for the reference arm, built by the oracle alone (its
+    scene generator, node producer and uniform derivation): this process maps
+    no library of the GPU implementation."""
+    from oracle import qbo
+    from qubatron_gb300 import scenes
+    w = scenes.WORKLOADS[workload_name]
+    t = time.time()
+    spec = scenes.SPECS[w.scene]
+    pts, nrm, col = qbo.scene_generate(spec.kind, spec.n_points, spec.seed, spec.n_boxes, spec.box, spec.n_spheres,
+                                       spec.sphere, spec.color_noise, spec.basesize, spec.levels)
+    nodes = qbo.build_tree(pts, spec.basesize, spec.levels)
+    scene = scenes.Scene(spec, pts, nrm, col, nodes)
+    views = scenes.workload_views(w, view_setup=qbo.view_setup)
+    character = scenes.make_character(w.character, root=w.character_root) if w.character else None
+    return w, scene, views, character, time.time() - t
+
+
+def mapped_repo_libraries() -> list:
+    """Shared libraries of this repository mapped into this process."""
+    out = set()
+    root = os.path.realpath(ROOT)
+    try:
+        with open("/proc/self/maps") as f:
+            for line in f:
+                path = os.path.realpath(line.rsplit(None, 1)[-1]) if "/" in line else ""
+                if path.startswith(root + os.sep) and ".so" in os.path.basename(path):
+                    out.add(os.path.relpath(path, root))
+    except OSError:
+        return ["unknown: /proc/self/maps unreadable"]
+    return sorted(out)
+
+
 def prepare(workload_name: str, host_nodes: bool = True):
     """Scene, views and character of a workload. House-scale scenes skip the
     host node array unless host_nodes; the GPU builds their tree."""
@@ -183,9 +240,8 @@ def cpu_sample(scene, views, budget_s: float, seed: int = 7, character=None, fra
     threads = os.cpu_count() or 1
     if character is not None:
         from qubatron_gb300 import scenes
-        from qubatron_gb300.octree import build_octree
         p, n = scenes.skin_reference(character, scenes.pose_bones(character, frame))
-        sc = qbo.Scene(scene.nodes, scene.colors, scene.normals, build_octree(p), character.colors, n)
+        sc = qbo.Scene(scene.nodes, scene.colors, scene.normals, qbo.build_tree(p), character.colors, n)
     else:
         sc = qbo.Scene(scene.nodes, scene.colors, scene.normals)
     ov = [qbo.QboView.from_bytes(v.to_bytes()) for v in views]
@@ -236,32 +292,37 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    w, scene, views, character, _ = prepare(WORKLOAD)
-    # each step: a bounded sample (~8 s) of the workload's pixels
-    from oracle import qbo  # noqa: F401
+    w, scene, views, character, prep_s = prepare_reference(WORKLOAD)
     times, rays_total = [], 0
     res = None
     for step in range(args.warmup + args.steps):
         # per step a bounded sample: 6 s of CPU work at most, warm-up steps 2 s
-        budget = min(args.cpu_seconds, 6.0) if step >= args.warmup else 2.0
+        budget = min(args.cpu_seconds, 6.0 if step >= args.warmup else 2.0)
         res = cpu_sample(scene, views, budget_s=budget, seed=100 + step, character=character, frame=step)
         if step >= args.warmup:
             times.append(res["seconds"])
             rays_total += res["rays"]
     value = rays_total / sum(times) / 1e6
+    libs = mapped_repo_libraries()
+    stray = [x for x in libs if not x.startswith("oracle" + os.sep)]
+    if stray:
+        raise RuntimeError(f"reference arm mapped libraries of the GPU implementation: {stray}")
     line = {
         "impl": "reference", "metric": "primary+shadow Mrays/s", "value": value, "unit": "Mrays/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * statistics.mean(times) if times else None, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-        "config": {"workload": WORKLOAD, "points": scene.points.shape[0], "nodes": int(scene.nodes.shape[0]),
-                   "resolution": f"{w.width}x{w.height}", "views": len(views), "depth": 12, "basecube": 1800.0},
+        "config": workload_config(w, scene, scene.nodes.shape[0], views),
         "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": res["cores"], "kind": res["kind"],
                          "sample": f"{args.steps} timed steps, {rays_total} rays in {sum(times):.1f} s; each step "
                                    f"a seeded pixel sample of the workload (last: {res['sample']})"},
         "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "libraries_mapped": libs,
+        "prep_seconds": round(prep_s, 1),
         "note": "the reference's own path is a GLSL fragment shader (no graphics stack here); this is its C "
-                "restatement (oracle/) on all host cores, per step a seeded pixel sample of the workload",
+                "restatement (oracle/) on all host cores, per step a seeded pixel sample of the workload; the "
+                "scene, node array and uniforms come from the oracle too, so no library of the GPU "
+                "implementation is loaded",
     }
     print(json.dumps(line))
     return 0
@@ -528,16 +589,9 @@ def run_gpu(args):
         "metric": "primary+shadow Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene)",
-        "config": {"workload": WORKLOAD, "points": int(scene.points.shape[0]), "nodes": n_nodes,
-                   "resolution": f"{w.width}x{w.height}" if w.width else "mixed", "views": len(views), "depth": 12,
-                   "basecube": 1800.0, "rays_per_step": rays, "nominal_2wh_rays_per_step": 2 * pixels,
-                   "dynamic_points": int(w.character),
-                   "per_step": "re-skin + rebuild dynamic tree + render" if chars else "render",
-                   "dynamic_update_ms": update_ms,
-                   "l2": "flushed between steps (2x L2 write, outside the timed events); node arrays "
-                         f"{n_nodes * 36 / 1e9:.2f} GB > L2",
-                   "parallelism": "replicas only" if world > 1 else "single GPU",
-                   "prep_seconds": round(prep_s, 1)},
+        "config": workload_config(w, scene, n_nodes, views),
+        "run": {"rays_per_step": rays, "nominal_2wh_rays_per_step": 2 * pixels, "dynamic_update_ms": update_ms,
+                "prep_seconds": round(prep_s, 1)},
         "e2e": e2e,
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
@@ -549,10 +603,10 @@ def run_gpu(args):
         "step_ms": [round(x, 4) for x in step_ms],
     }
     if proposal is not None:
-        line["config"]["per_step"] = "two-pass render with occluder-network proposals (network evaluated every step)"
+        line["run"]["per_step"] = "two-pass render with occluder-network proposals (network evaluated every step)"
         line["proposal"] = proposal
-    line["config"]["launch"] = "CUDA graph replay (qbc_graph_launch)" if use_graph else "eager (qbc_render_views*)"
-    line["config"]["tuning"] = tuning
+    line["run"]["launch"] = "CUDA graph replay (qbc_graph_launch)" if use_graph else "eager (qbc_render_views*)"
+    line["run"]["tuning"] = tuning
     for g in graphs:
         g.close()
     if rank == 0 and not args.no_cpu_baseline:

@@ -215,6 +215,18 @@ typedef struct qbc_ray_hits
 int qbc_trace_rays(qbc_ctx* ctx, const float* pos, const float* dir, int64_t n, const float basecube[4], int maxlevel, const qbc_ray_hits* out, int on_device);
 
 /*
+ * Camera rays of selected pixels of one view, exactly as the render kernels
+ * generate them (octree_fsh.c:401-418: ctp = pixel centre in the render's
+ * coordinate space, csv = qx * (qz * (ctp - cfp)), and the flare test's
+ * argument dot(normalize(light - camfp), normalize(csv))). Per pixel k,
+ * out[4k..4k+3] = (csv.x, csv.y, csv.z, cosine). px, py and out are host
+ * arrays (on_device = 0) or device arrays of the context's GPU. Lets a caller
+ * check the per-pixel ray against its own camera math (the reference's
+ * mt_quat.c quaternions) and find pixels on the flare threshold.
+ */
+int qbc_camera_rays(qbc_ctx* ctx, const qbc_view* view, const int32_t* px, const int32_t* py, int64_t n, float* out, int on_device);
+
+/*
  * Render without allocating anything (no counterpart in the reference).
  *
  * For callers that cannot call cudaMalloc while they render: a frame loop

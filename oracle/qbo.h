@@ -131,6 +131,10 @@ void qbo_trace(const qbo_scene* sc, const float basecube[4], int maxlevel, const
 /* One fragment: main() (octree_fsh.c:399-464) at pixel (i, j), j from the bottom. */
 void qbo_shade_pixel(const qbo_scene* sc, const qbo_view* v, int i, int j, float rgba[4], uint32_t* flags, int32_t leaf[4], float isp[4], uint32_t visits[4]);
 
+/* Camera ray of pixel (i, j) (octree_fsh.c:401-418): out = (csv, cosine of
+ * the angle between csv and light - camfp). */
+void qbo_camera_ray(const qbo_view* v, int i, int j, float out[4]);
+
 /* A whole frame, OpenMP over 8x8 pixel tiles; threads <= 0 uses all. */
 void qbo_render(const qbo_scene* sc, const qbo_view* v, const qbo_frame* out, int threads);
 
@@ -165,6 +169,13 @@ int  qbo_insert_point(int32_t* nodes, int64_t* len, int64_t cap, float basesize,
 int  qbo_insert_path(int32_t* nodes, int64_t* len, int64_t cap, int levels, int64_t modind, const int32_t* octets);
 void qbo_remove_point(int32_t* nodes, float basesize, int levels, const float pnt[3], int32_t* modind, int32_t* octind);
 void qbo_point_octets(float basesize, int levels, const float pnt[3], int32_t* octets);
+/* All n points in order into an empty tree; returns the node count or -1. */
+int64_t qbo_build_tree(const float* pnts, int64_t n, float basesize, int levels, int32_t* nodes, int64_t cap);
+
+/* Seeded synthetic scenes of the benchmark workloads (qbo_scene.c; kind 0
+ * floor, 1 room, 2 house): n float3 points, normals and colours in
+ * octree-path order. Returns 0, or a negative value on bad arguments. */
+int qbo_scene_generate(int kind, int levels, int64_t n, uint64_t seed, float basesize, int n_boxes, float box_min, float box_max, int n_spheres, float sphere_min, float sphere_max, float color_noise, float* pnts, float* nrms, float* cols);
 
 #ifdef __cplusplus
 }

@@ -16,7 +16,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIBQBO = os.path.join(HERE, "_build", "libqbo.so")
 LIBREF = os.path.join(HERE, "_ref", "libqbref.so")
-REFERENCE_ROOT = os.environ.get("QB_REFERENCE_ROOT", "/root/reference")
+# the reference checkout the pinning build compiles from: QB_REFERENCE_ROOT,
+# or None (no reference build; the committed golden fixtures still pin)
+REFERENCE_ROOT = os.environ.get("QB_REFERENCE_ROOT") or None
 
 f32p = C.POINTER(C.c_float)
 i32p = C.POINTER(C.c_int32)
@@ -81,9 +83,11 @@ def build_oracle() -> str:
     return LIBQBO
 
 
-def build_reference(root: str = REFERENCE_ROOT) -> str | None:
-    """Compile the reference's octree.c into oracle/_ref when its sources exist."""
-    if not os.path.isfile(os.path.join(root, "src", "qubatron", "octree.c")):
+def build_reference(root: str | None = None) -> str | None:
+    """Compile the reference's octree.c into oracle/_ref when its sources exist
+    under root (default QB_REFERENCE_ROOT; None when neither is given)."""
+    root = root or REFERENCE_ROOT
+    if not root or not os.path.isfile(os.path.join(root, "src", "qubatron", "octree.c")):
         return None
     res = subprocess.run([os.path.join(HERE, "build_ref.sh"), root], capture_output=True, text=True)
     if res.returncode != 0:
@@ -119,6 +123,13 @@ def qbo() -> C.CDLL:
         lib.qbo_build_boxes.argtypes = [i32p, C.c_int64, u32p]
         lib.qbo_build_boxes.restype = C.c_int32
         lib.qbo_point_octets.restype = None
+        lib.qbo_build_tree.argtypes = [f32p, C.c_int64, C.c_float, C.c_int, i32p, C.c_int64]
+        lib.qbo_build_tree.restype = C.c_int64
+        lib.qbo_scene_generate.argtypes = [C.c_int, C.c_int, C.c_int64, C.c_uint64, C.c_float, C.c_int, C.c_float,
+                                           C.c_float, C.c_int, C.c_float, C.c_float, C.c_float, f32p, f32p, f32p]
+        lib.qbo_scene_generate.restype = C.c_int
+        lib.qbo_camera_ray.argtypes = [C.POINTER(QboView), C.c_int, C.c_int, f32p]
+        lib.qbo_camera_ray.restype = None
         _qbo = lib
     return _qbo
 
@@ -145,6 +156,10 @@ def ref() -> C.CDLL | None:
         lib.qbref_load_flat.argtypes = [C.c_char_p] * 4 + [f32p, f32p, f32p, C.c_long, i32p, C.c_long,
                                                            C.POINTER(C.c_long)]
         lib.qbref_load_flat.restype = C.c_long
+        lib.qbref_frame_quats.argtypes = [C.c_float, C.c_float, f32p, f32p]
+        lib.qbref_frame_quats.restype = None
+        lib.qbref_camera_dirs.argtypes = [f32p, f32p, f32p, f32p, C.c_long, f32p]
+        lib.qbref_camera_dirs.restype = None
         _ref = lib
     return _ref
 
@@ -239,18 +254,30 @@ def render_pixels(scene: Scene, view: QboView, px: np.ndarray, py: np.ndarray, t
     return out
 
 
-def build_tree(points: np.ndarray, basesize: float, levels: int) -> np.ndarray:
-    """octree_insert_point restatement over all points in order."""
+def build_tree(points: np.ndarray, basesize: float = 1800.0, levels: int = 12) -> np.ndarray:
+    """octree_insert_point restatement over all points in order (model
+    indices 0..n-1), in one C call."""
     pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
     cap = 1 + pts.shape[0] * levels
-    nodes = np.zeros(cap * 12, np.int32)
-    length = C.c_int64(1)
-    lib = qbo()
-    for i in range(pts.shape[0]):
-        rc = lib.qbo_insert_point(nodes.ctypes.data_as(i32p), C.byref(length), cap, basesize, levels, i,
-                                  pts[i].ctypes.data_as(f32p), None)
-        assert rc == 0
-    return nodes[: length.value * 12].reshape(-1, 12).copy()
+    nodes = np.empty(cap * 12, np.int32)
+    length = qbo().qbo_build_tree(pts.ctypes.data_as(f32p), pts.shape[0], basesize, levels,
+                                  nodes.ctypes.data_as(i32p), cap)
+    assert length > 0
+    return nodes[: length * 12].reshape(-1, 12).copy()
+
+
+def scene_generate(kind: int, n_points: int, seed: int, n_boxes: int, box, n_spheres: int, sphere,
+                   color_noise: float = 0.0, basesize: float = 1800.0, levels: int = 12):
+    """The benchmark's seeded synthetic scene (points, normals, colours in
+    octree-path order), the same bits as the library's qbc_scene_generate."""
+    pts, nrm, col = (np.empty((n_points, 3), np.float32) for _ in range(3))
+    rc = qbo().qbo_scene_generate(int(kind), int(levels), int(n_points), int(seed), float(basesize), int(n_boxes),
+                                  float(box[0]), float(box[1]), int(n_spheres), float(sphere[0]), float(sphere[1]),
+                                  float(color_noise), pts.ctypes.data_as(f32p), nrm.ctypes.data_as(f32p),
+                                  col.ctypes.data_as(f32p))
+    if rc != 0:
+        raise ValueError(f"qbo_scene_generate failed ({rc})")
+    return pts, nrm, col
 
 
 def build_tree_paths(octets: np.ndarray, levels: int) -> np.ndarray:
@@ -319,3 +346,33 @@ def ref_load_flat(prefix: str) -> dict:
     lib.qbref_load_flat(*paths, vtx.ctypes.data_as(f32p), col.ctypes.data_as(f32p), nrm.ctypes.data_as(f32p), n,
                         rng.ctypes.data_as(i32p), rng.size, C.byref(rc))
     return {"points": vtx, "colors": col, "normals": nrm, "ranges": rng[:rc.value]}
+
+
+def camera_rays(view: QboView, px, py) -> np.ndarray:
+    """The oracle's camera ray per pixel: (n, 4) csv xyz and the flare test's
+    cosine."""
+    px = np.asarray(px, np.int32).ravel()
+    py = np.asarray(py, np.int32).ravel()
+    out = np.zeros((px.size, 4), np.float32)
+    lib = qbo()
+    for k in range(px.size):
+        lib.qbo_camera_ray(C.byref(view), int(px[k]), int(py[k]), out[k].ctypes.data_as(f32p))
+    return out
+
+
+def ref_frame_quats(angle_x: float, angle_y: float):
+    """The reference's mt_quat.c frame quaternions (qz, qx) of a camera angle."""
+    qz = np.zeros(4, np.float32)
+    qx = np.zeros(4, np.float32)
+    ref().qbref_frame_quats(angle_x, angle_y, qz.ctypes.data_as(f32p), qx.ctypes.data_as(f32p))
+    return qz, qx
+
+
+def ref_camera_dirs(qz, qx, cfp, ctp) -> np.ndarray:
+    """The reference's mt_quat.c rotation of screen points ctp (n, 2) - cfp."""
+    qz, qx, cfp = (np.ascontiguousarray(a, np.float32) for a in (qz, qx, cfp))
+    ctp = np.ascontiguousarray(ctp, np.float32).reshape(-1, 2)
+    out = np.zeros((ctp.shape[0], 3), np.float32)
+    ref().qbref_camera_dirs(qz.ctypes.data_as(f32p), qx.ctypes.data_as(f32p), cfp.ctypes.data_as(f32p),
+                            ctp.ctypes.data_as(f32p), ctp.shape[0], out.ctypes.data_as(f32p))
+    return out

@@ -467,6 +467,23 @@ void qbo_view_setup(float width, float height, const float position[3], const fl
     v->shoot    = shoot;
 }
 
+void qbo_camera_ray(const qbo_view* v, int i, int j, float out[4])
+{
+    /* ray generation (octree_fsh.c:402-413); coord is the pixel centre */
+    float cx     = ((float) i + 0.5f) * v->coord_scale[0];
+    float cy     = ((float) j + 0.5f) * v->coord_scale[1];
+    float csv[3] = {cx - v->cfp[0], cy - v->cfp[1], 0.0f - v->cfp[2]};
+    quat_rotate(v->qz, csv);
+    quat_rotate(v->qx, csv);
+    /* camangle's argument (octree_fsh.c:416-417) */
+    float ncsv[3];
+    normalize3(csv, ncsv);
+    out[0] = csv[0];
+    out[1] = csv[1];
+    out[2] = csv[2];
+    out[3] = dot3(v->ncamlight, ncsv);
+}
+
 void qbo_shade_pixel(const qbo_scene* sc, const qbo_view* v, int i, int j, float rgba[4], uint32_t* flags, int32_t leaf[4], float isp[4], uint32_t visits[4])
 {
     uint32_t f = 0;
@@ -475,16 +492,10 @@ void qbo_shade_pixel(const qbo_scene* sc, const qbo_view* v, int i, int j, float
     visits[0] = visits[1] = visits[2] = visits[3] = 0;
     rgba[0] = rgba[1] = rgba[2] = rgba[3] = 0.0f;
 
-    /* ray generation (octree_fsh.c:402-413); coord is the pixel centre */
-    float cx     = ((float) i + 0.5f) * v->coord_scale[0];
-    float cy     = ((float) j + 0.5f) * v->coord_scale[1];
-    float csv[3] = {cx - v->cfp[0], cy - v->cfp[1], 0.0f - v->cfp[2]};
-    quat_rotate(v->qz, csv);
-    quat_rotate(v->qx, csv);
-
-    float ncsv[3];
-    normalize3(csv, ncsv);
-    float cosang = dot3(v->ncamlight, ncsv);
+    float ray[4];
+    qbo_camera_ray(v, i, j, ray);
+    float csv[3]  = {ray[0], ray[1], ray[2]};
+    float cosang = ray[3];
     int   flare  = cosang > v->flare_cos && cosang <= 1.0f;
 
     qbo_hit res;

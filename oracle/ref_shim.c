@@ -8,6 +8,7 @@
  */
 #include "octree.c" /* declarations only: included below level 0 */
 #include "model.c"
+#include "mt_quat.c"
 
 #include <string.h>
 
@@ -97,4 +98,33 @@ long qbref_load_flat(const char* pnt, const char* col, const char* nrm, const ch
     *range_count = m.range_count;
     if (ranges != NULL && m.range_count <= rcap) memcpy(ranges, m.ranges, (size_t) m.range_count * sizeof(int));
     return n;
+}
+
+/* The frame quaternions of the shader's main() (octree_fsh.c:406-408) with the
+ * reference's C quaternion functions (mt_quat.c:14-29, the same formulas as
+ * the shader's quat_from_axis_angle / quat_rotate at octree_fsh.c:381-395):
+ * qz about +y by -angle.x, qx about qz-rotated -x by -angle.y. */
+void qbref_frame_quats(float angle_x, float angle_y, float* qz, float* qx)
+{
+    v4_t z  = quat_from_axis_angle((v3_t){0.0f, 1.0f, 0.0f}, -angle_x);
+    v3_t vx = quat_rotate(z, (v3_t){-1.0f, 0.0f, 0.0f});
+    v4_t x  = quat_from_axis_angle(vx, -angle_y);
+    qz[0] = z.x, qz[1] = z.y, qz[2] = z.z, qz[3] = z.w;
+    qx[0] = x.x, qx[1] = x.y, qx[2] = x.z, qx[3] = x.w;
+}
+
+/* csv = quat_rotate(qx, quat_rotate(qz, ctp - cfp)) (octree_fsh.c:402-413)
+ * for n screen points ctp (x, y; z = 0). */
+void qbref_camera_dirs(const float* qz, const float* qx, const float* cfp, const float* ctp, long n, float* out)
+{
+    v4_t z = {qz[0], qz[1], qz[2], qz[3]}, x = {qx[0], qx[1], qx[2], qx[3]};
+    for (long i = 0; i < n; i++)
+    {
+        v3_t csv = v3_sub((v3_t){ctp[2 * i], ctp[2 * i + 1], 0.0f}, (v3_t){cfp[0], cfp[1], cfp[2]});
+        csv      = quat_rotate(z, csv);
+        csv      = quat_rotate(x, csv);
+        out[3 * i + 0] = csv.x;
+        out[3 * i + 1] = csv.y;
+        out[3 * i + 2] = csv.z;
+    }
 }

@@ -198,6 +198,8 @@ SIGNATURES = {
     "qbc_render_views": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int, C.c_int]),
     "qbc_trace_rays": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, c_float_p, C.c_int,
                                  C.POINTER(RayHits), C.c_int]),
+    "qbc_camera_rays": (C.c_int, [C.c_void_p, C.POINTER(View), C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                  C.c_int]),
     "qbc_render_views_ex": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int, C.c_int,
                                       C.POINTER(RenderOpts), C.POINTER(RenderStats)]),
     "qbc_render_views_noalloc": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int]),

@@ -979,6 +979,59 @@ extern "C" int qbc_trace_rays(qbc_ctx* c, const float* pos, const float* dir, in
   return QBC_OK;
 }
 
+namespace qbc {
+
+// Camera rays of selected pixels of one view: (csv, cos of the angle to the
+// light) per pixel, from the same camera_ray the render kernels call.
+__global__ void camera_rays_kernel(const __grid_constant__ qbc_view v, const int32_t* px, const int32_t* py,
+                                   int64_t n, float4* out) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+    out[k] = camera_ray(v, px[k], py[k]);
+}
+
+}  // namespace qbc
+
+extern "C" int qbc_camera_rays(qbc_ctx* c, const qbc_view* view, const int32_t* px, const int32_t* py, int64_t n,
+                               float* out, int on_device) {
+  qbc::clear_error();
+  if (!c || !view || (n > 0 && (!px || !py || !out))) return fail(QBC_E_ARG, "qbc_camera_rays: null argument");
+  if (n < 0) return fail(QBC_E_ARG, "qbc_camera_rays: negative pixel count");
+  int rc = check_view(*view, 0);
+  if (rc) return rc;
+  if (n == 0) return QBC_OK;
+  QBC_CUDA(cudaSetDevice(c->device));
+  const int32_t* dpx = px;
+  const int32_t* dpy = py;
+  float4* dout = reinterpret_cast<float4*>(out);
+  if (!on_device) {
+    // pixel indices and rays staged in the context's scratch
+    const size_t idx = ((size_t)n * 4 + 255) & ~size_t(255);
+    const size_t need = 2 * idx + (size_t)n * 16;
+    if (need > c->scratch_bytes) {
+      if (c->scratch) QBC_CUDA(cudaFree(c->scratch));
+      c->scratch = nullptr;
+      c->scratch_bytes = 0;
+      cudaError_t e = cudaMalloc(&c->scratch, need);
+      if (e != cudaSuccess) return fail(QBC_E_NOMEM, "camera-ray scratch of %zu bytes: %s", need, cudaGetErrorString(e));
+      c->scratch_bytes = need;
+    }
+    char* base = (char*)c->scratch;
+    QBC_CUDA(cudaMemcpyAsync(base, px, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+    QBC_CUDA(cudaMemcpyAsync(base + idx, py, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+    dpx = (const int32_t*)base;
+    dpy = (const int32_t*)(base + idx);
+    dout = (float4*)(base + 2 * idx);
+  }
+  qbc::camera_rays_kernel<<<launch_grid(c, n), 256, 0, c->stream>>>(*view, dpx, dpy, n, dout);
+  QBC_CUDA(cudaGetLastError());
+  ++c->launches;
+  if (!on_device) {
+    QBC_CUDA(cudaMemcpyAsync(out, dout, (size_t)n * 16, cudaMemcpyDeviceToHost, c->stream));
+    QBC_CUDA(cudaStreamSynchronize(c->stream));
+  }
+  return QBC_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Render without allocating (qbc_render_views_noalloc)
 // ---------------------------------------------------------------------------

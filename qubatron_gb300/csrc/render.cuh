@@ -60,6 +60,25 @@ __device__ __forceinline__ float3 quat_rotate(const float* q, float3 v) {
   return make_float3(v.x + 2.0f * c2x, v.y + 2.0f * c2y, v.z + 2.0f * c2z);
 }
 
+// Camera ray of pixel (i, j) of a view (octree_fsh.c:401-418): the screen
+// vector ctp - cfp rotated by the yaw and pitch quaternions (csv), and the
+// cosine of its angle to the light direction (the flare test's argument).
+__device__ __forceinline__ float4 camera_ray(const qbc_view& v, int i, int j) {
+  float cx = ((float)i + 0.5f) * v.coord_scale[0];
+  float cy = ((float)j + 0.5f) * v.coord_scale[1];
+  float3 csv = make_float3(cx - v.cfp[0], cy - v.cfp[1], 0.0f - v.cfp[2]);
+  csv = quat_rotate(v.qz, csv);
+  csv = quat_rotate(v.qx, csv);
+  float3 ncsv = normalize3(csv);
+  float cosang = dot3(make_float3(v.ncamlight[0], v.ncamlight[1], v.ncamlight[2]), ncsv);
+  return make_float4(csv.x, csv.y, csv.z, cosang);
+}
+
+// The flare test acos(cosang) < 0.02 as a cosine threshold.
+__device__ __forceinline__ bool flare_wanted(const qbc_view& v, float cosang) {
+  return cosang > v.flare_cos && cosang <= 1.0f;
+}
+
 // GL float -> unorm8 for the RGBA8 colour target.
 __device__ __forceinline__ uint32_t unorm8(float f) {
   if (!(f > 0.0f)) return 0u;
@@ -220,14 +239,9 @@ struct Shader {
     const qbc_view& v = batch.job[vi].v;
     maxlevel = v.maxlevel;
     bc = held_bc<EXACT>(v);
-    float cx = ((float)i + 0.5f) * v.coord_scale[0];
-    float cy = ((float)j + 0.5f) * v.coord_scale[1];
-    float3 csv = make_float3(cx - v.cfp[0], cy - v.cfp[1], 0.0f - v.cfp[2]);
-    csv = quat_rotate(v.qz, csv);
-    csv = quat_rotate(v.qx, csv);
-    float3 ncsv = normalize3(csv);
-    float cosang = dot3(make_float3(v.ncamlight[0], v.ncamlight[1], v.ncamlight[2]), ncsv);
-    px.w(kPxFlags) = (cosang > v.flare_cos && cosang <= 1.0f) ? kWantFlare : 0u;
+    const float4 ray = camera_ray(v, i, j);
+    const float3 csv = make_float3(ray.x, ray.y, ray.z);
+    px.w(kPxFlags) = flare_wanted(v, ray.w) ? kWantFlare : 0u;
     px.f(kPxCsv) = csv.x;
     px.f(kPxCsv + 1) = csv.y;
     px.f(kPxCsv + 2) = csv.z;

@@ -230,6 +230,17 @@ class OctreeGLC:
                                        int(maxlevel), C.byref(h), 0))
         return out
 
+    def camera_rays(self, view: View, px: np.ndarray, py: np.ndarray) -> np.ndarray:
+        """Camera rays of the pixels (px, py) of a view as the render kernels
+        make them (qbc_camera_rays): (n, 4) float32, csv xyz and the cosine of
+        its angle to the light."""
+        px = np.ascontiguousarray(px, np.int32).ravel()
+        py = np.ascontiguousarray(py, np.int32).ravel()
+        out = np.zeros((px.size, 4), np.float32)
+        check(self._lib.qbc_camera_rays(self.handle, C.byref(view), C.c_void_p(px.ctypes.data),
+                                        C.c_void_p(py.ctypes.data), px.size, C.c_void_p(out.ctypes.data), 0))
+        return out
+
     def set_stream(self, stream_ptr: Optional[int]) -> None:
         check(self._lib.qbc_set_stream(self.handle, C.c_void_p(stream_ptr or 0)))
 

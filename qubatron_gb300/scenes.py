@@ -251,10 +251,12 @@ def train_views(w: Workload, maxlevel: int = LEVELS, basesize: float = BASESIZE)
                        vertical_fov_focal(th, w.fov_deg) if w.fov_deg else 0.0) for pos, ang in (w.train_poses or [])]
 
 
-def workload_views(w: Workload, maxlevel: int = LEVELS, basesize: float = BASESIZE):
+def workload_views(w: Workload, maxlevel: int = LEVELS, basesize: float = BASESIZE, view_setup=None):
     """qbc_view per pose: the reference's uniforms with the configured
-    vertical field of view."""
-    from .octree_glc import view_setup
+    vertical field of view. view_setup derives them (default: the library's
+    qbc_view_setup; any function with its arguments and struct layout)."""
+    if view_setup is None:
+        from .octree_glc import view_setup
     sizes = w.sizes or [(w.width, w.height)] * len(w.poses)
     return [view_setup(sw, sh, pos, ang, w.lighta, w.quality, maxlevel, basesize, 0,
                        vertical_fov_focal(sh, w.fov_deg) if w.fov_deg else 0.0)

@@ -1,8 +1,10 @@
 """Generate the golden fixtures in tests/golden from the reference itself.
 
-Run in a checkout that has the reference sources (default /root/reference):
+Run where the reference sources are checked out, giving that checkout:
 
-    python tests/golden/make_golden.py [REFERENCE_ROOT]
+    python tests/golden/make_golden.py REFERENCE_ROOT
+
+(or set QB_REFERENCE_ROOT).
 
 It compiles the reference's src/qubatron/octree.c and model.c
 (oracle/build_ref.sh) and
@@ -20,6 +22,8 @@ records what that code produces:
                        tree for duplicates, misses and points just below 0
                        (walks the reference defines), with the node array
                        after each call sequence;
+* ``camera_quat.npz``  frame quaternions and per-pixel camera rays from the
+                       reference's mt_quat.c (--camera-only makes just this);
 * ``flat/small.{pnt,col,nrm,rng}`` + ``flat_small.npz``  a 2,000-point qmc
                        flat model (7 trailing bytes after the last point, a
                        partial int after the last range) and what the
@@ -111,9 +115,60 @@ def floor_points(n: int):
     return pts, nrm, col
 
 
-def main(root: str) -> None:
+def camera_golden() -> None:
+    """camera_quat.npz: the frame quaternions and per-pixel camera rays of the
+    shader's ray generation (octree_fsh.c:401-413), computed with the
+    reference's own C quaternion functions (src/mt_math/mt_quat.c:14-29) for
+    the benchmark poses and edge angles. The render size, focus point and pixel
+    centres come from the oracle's uniform derivation; the rotation is the
+    reference's."""
+    from qubatron_gb300 import scenes
+    cams = []  # (width, height, quality, focal, position, angle)
+    for name in ("room20m_1920x1080x16", "floor1m_mlp_1920x1080x16"):
+        w = scenes.WORKLOADS[name]
+        for pos, ang in w.poses:
+            cams.append((w.width, w.height, w.quality, scenes.vertical_fov_focal(w.height), pos, ang))
+    w = scenes.WORKLOADS["floor1m_char2m_mixed_x64"]
+    for (sw, sh), (pos, ang) in list(zip(w.sizes, w.poses))[:16]:
+        cams.append((sw, sh, w.quality, scenes.vertical_fov_focal(sh), pos, ang))
+    for yaw in (0.0, 1e-7, 1.5707964, -1.5707964, 3.1415927, -3.1415927, 3.0, -2.5):
+        for pitch in (0.0, -0.4, 0.15, 1.5, -1.5):
+            # reference focal length; quality 3 gives a fractional render size
+            cams.append((1280, 720, 10 if pitch != 0.15 else 3, 0.0, (903.7, 421.3, 1702.9), (yaw, pitch, 0.0)))
+    rng = np.random.default_rng(16)
+    rows = {k: [] for k in ("view", "px", "py", "ctp", "csv")}
+    angles, qzs, qxs, dims = [], [], [], []
+    for vi, (sw, sh, q, focal, pos, ang) in enumerate(cams):
+        v = qbo.view_setup(float(sw), float(sh), pos, ang, 0.0, q, 12, S, 0, focal)
+        qz, qx = qbo.ref_frame_quats(ang[0], ang[1])
+        W, H = v.width_px, v.height_px
+        px = np.concatenate([[0, W - 1, 0, W - 1, W // 2], rng.integers(0, W, 27)]).astype(np.int32)
+        py = np.concatenate([[0, 0, H - 1, H - 1, H // 2], rng.integers(0, H, 27)]).astype(np.int32)
+        # pixel centres as the oracle and the kernels form them
+        ctp = np.stack([(px.astype(np.float32) + np.float32(0.5)) * np.float32(v.coord_scale[0]),
+                        (py.astype(np.float32) + np.float32(0.5)) * np.float32(v.coord_scale[1])], 1)
+        csv = qbo.ref_camera_dirs(qz, qx, np.array(v.cfp, np.float32), ctp)
+        angles.append(ang[:2])
+        qzs.append(qz)
+        qxs.append(qx)
+        dims.append((sw, sh, q, focal, *pos))
+        rows["view"].append(np.full(px.size, vi, np.int32))
+        rows["px"].append(px)
+        rows["py"].append(py)
+        rows["ctp"].append(ctp)
+        rows["csv"].append(csv)
+    np.savez_compressed(os.path.join(HERE, "camera_quat.npz"), angle=np.array(angles, np.float32),
+                        qz=np.array(qzs, np.float32), qx=np.array(qxs, np.float32), cam=np.array(dims, np.float64),
+                        **{k: np.concatenate(v) for k, v in rows.items()})
+    print("camera_quat:", len(cams), "cameras,", sum(a.size for a in rows["px"]), "pixels")
+
+
+def main(root: str, only=None) -> None:
     if qbo.build_reference(root) is None:
         raise SystemExit(f"reference sources not found under {root}")
+    if only == "camera":
+        camera_golden()
+        return
 
     # ---- 5-point scene ----
     nodes5 = qbo.ref_build(FIVE_POINTS, S, LEVELS)
@@ -187,6 +242,12 @@ def main(root: str) -> None:
     np.savez_compressed(os.path.join(HERE, "flat_small.npz"), **got)
     print("flat_small:", got["points"].shape[0], "points,", got["ranges"].size, "range ints")
 
+    camera_golden()
+
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else qbo.REFERENCE_ROOT)
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    root = args[0] if args else qbo.REFERENCE_ROOT
+    if not root:
+        raise SystemExit("usage: make_golden.py REFERENCE_ROOT [--camera-only] (or set QB_REFERENCE_ROOT)")
+    main(root, "camera" if "--camera-only" in sys.argv else None)

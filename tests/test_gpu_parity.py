@@ -263,3 +263,30 @@ def test_out_of_range_indices_are_flagged(ctx, oracle):
     sc = oracle_scene(oracle, nodes, col, nrm)
     v = view_setup(200, 150, (900.0, 900.0, 3000.0), (0.0, 0.0, 0.0), 0.0, 10, LEVELS, S, 0, 0.0)
     compare_frame(gpu_frame(ctx, v), oracle.render(sc, _view_for_oracle(oracle, v)), "oob")
+
+
+def test_camera_rays_match_mt_quat(lib, oracle, ctx):
+    """The kernels' per-pixel camera ray (the function the render kernels
+    call) against the rays the reference's mt_quat.c computes from the same
+    frame quaternions (tests/golden/camera_quat.npz), bit for bit; the flare
+    test's cosine against the oracle. The quaternions are taken from the
+    fixture, so the check does not depend on the host's sinf."""
+    import os
+
+    import qubatron_gb300 as qb
+    from conftest import GOLDEN
+    g = dict(np.load(os.path.join(GOLDEN, "camera_quat.npz")))
+    for vi in range(g["angle"].shape[0]):
+        sw, sh, q, focal, x, y, z = g["cam"][vi]
+        args = (float(sw), float(sh), (float(x), float(y), float(z)),
+                (float(g["angle"][vi][0]), float(g["angle"][vi][1]), 0.0), 0.0, int(q), 12, S, 0, float(focal))
+        v = qb.view_setup(*args)
+        for k in range(4):
+            v.qz[k] = float(g["qz"][vi][k])
+            v.qx[k] = float(g["qx"][vi][k])
+        m = g["view"] == vi
+        got = ctx.camera_rays(v, g["px"][m], g["py"][m])
+        np.testing.assert_array_equal(got[:, :3].view(np.uint32), g["csv"][m].view(np.uint32),
+                                      err_msg=f"camera {vi}")
+        ref = oracle.camera_rays(_view_for_oracle(oracle, v), g["px"][m], g["py"][m])
+        np.testing.assert_array_equal(got.view(np.uint32), ref.view(np.uint32), err_msg=f"camera {vi} cosine")
