@@ -275,6 +275,7 @@ def cpu_sample(scene, views, budget_s: float, seed: int = 7, character=None, fra
                      f"({rays} rays, {dt:.1f} s)",
            "seconds": dt, "rays": rays}
     if gpu_frames is not None:
+        res["kept"] = kept
         # the GPU frame's row is py counted from the bottom (GL order), as the
         # oracle's pixel coordinates
         n = bad8 = badf = badl = 0
@@ -357,6 +358,161 @@ def measure_e2e(ctx, views, rays, world, flush, steps, update=None, render=None)
     h2d = len(views) * 132  # qbc_view uniforms, passed as launch parameters
     return {"value": rate / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "ms_per_step": 1000.0 * slowest_s / len(e2e_t)}
+
+
+def time_steps(fn, stream, flush, warmup: int, steps: int):
+    """warmup untimed calls, then steps calls each bracketed by CUDA events
+    on `stream`, L2 flushed before each (outside the events); per-step ms."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for a, b in ev:
+        flush.zero_()
+        a.record(stream)
+        fn()
+        b.record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in ev]
+
+
+PROPOSAL_WORKLOAD = "floor1m_mlp_1920x1080x16"
+
+
+def proposal_comparison(args, device: int, stream, flush) -> dict:
+    """The metric's own comparison on the learned-proposal workload (the floor
+    scene, 16 held-out poses at 1920x1080): the occluder network is trained
+    on the plain walk's logged shadow rays of 256 other poses (untimed), then
+    four arms render the same frames, each tuned by qbc_autotune and replayed
+    as a CUDA graph: plain fused persistent, plain two-pass persistent, the
+    two-pass frame with network proposals, and the plain one-thread-per-pixel
+    schedule. Every arm's pixels are checked against the oracle on a seeded
+    sample."""
+    import torch
+    import qubatron_gb300 as qb
+    from qubatron_gb300 import scenes
+    w = scenes.WORKLOADS[PROPOSAL_WORKLOAD]
+    scene = scenes.make_scene(w.scene)
+    views = scenes.workload_views(w)
+    ctx = qb.OctreeGLC(device)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.upload_model(False, scene.colors, scene.normals)
+    ctx.upload_octree(False, scene.nodes)
+    lib = qb._lib
+    out = {"workload": w.name, "points": int(scene.points.shape[0]), "nodes": int(scene.nodes.shape[0]),
+           "views": len(views), "resolution": f"{w.width}x{w.height}"}
+    try:
+        tv = scenes.train_views(w)
+        t0 = time.time()
+        samples = 0
+        for i in range(0, len(tv), 32):
+            samples = ctx.proposal_collect(tv[i:i + 32])
+        collect_s = time.time() - t0
+        t0 = time.time()
+        st = ctx.proposal_train(steps=args.train_steps, batch=8192, lr=2e-3, seed=1)
+        torch.cuda.synchronize()
+        out["training"] = {"poses": len(tv), "pose_size": "%dx%d" % w.train_size, "samples": samples,
+                           "occluded": st["occluded"], "steps": args.train_steps, "batch": 8192,
+                           "loss_first": st["loss_first"], "loss_last": st["loss_last"],
+                           "collect_s": round(collect_s, 2), "train_s": round(time.time() - t0, 2)}
+        ctx.set_option(lib.OPT_PROPOSAL_GATE, args.proposal_gate)
+        ctx.set_option(lib.OPT_PROPOSAL_COUNT, args.proposal_count)
+        out["proposal_options"] = {"gate_per_mille": args.proposal_gate, "count": args.proposal_count,
+                                   "level": args.proposal_level}
+
+        frames = [torch.empty((v.height_px, v.width_px, 4), dtype=torch.uint8, device="cuda") for v in views]
+        outs = []
+        for f in frames:
+            o = qb.Outputs()
+            o.rgba8 = f.data_ptr()
+            outs.append(o)
+        # rays of a frame (the same for every arm: same pixels)
+        flags = [torch.empty((v.height_px, v.width_px), dtype=torch.int32, device="cuda") for v in views]
+        inst = []
+        for f, fl in zip(frames, flags):
+            o = qb.Outputs()
+            o.rgba8, o.flags = f.data_ptr(), fl.data_ptr()
+            inst.append(o)
+        ctx.render_views(views, inst, on_device=True)
+        torch.cuda.synchronize()
+        rays = sum(count_rays(fl.cpu().numpy().view(np.uint32)) for fl in flags)
+        out["rays_per_frame"] = rays
+
+        mlp_kw = dict(two_pass=True, proposals=lib.PROPOSE_MLP, proposal_level=args.proposal_level)
+        arms = [("plain_fused", {}, 1), ("plain_two_pass", {"two_pass": True}, 1), ("learned", mlp_kw, 1),
+                ("plain_simple", {}, 0)]
+        base = (ctx.get_option(lib.OPT_TILE_WIDTH), ctx.get_option(lib.OPT_BLOCKS_PER_SM),
+                ctx.get_option(lib.OPT_SERVICE_MIN))
+        res = {}
+        for name, kw, persistent in arms:
+            ctx.set_option(lib.OPT_TILE_WIDTH, base[0])
+            ctx.set_option(lib.OPT_BLOCKS_PER_SM, base[1])
+            ctx.set_option(lib.OPT_SERVICE_MIN, base[2])
+            ctx.set_option(lib.OPT_PERSISTENT, persistent)
+            tuning = ctx.autotune(views, outs, reps=3, **kw) if args.autotune else None
+            g = ctx.graph_capture(views, outs, **kw)
+            ms = time_steps(g.launch, stream, flush, args.warmup, args.steps)
+            g.close()
+            # this arm's pixels for the parity sample
+            chk = {k: [] for k in ("rgba8", "flags", "leaf")}
+            couts = []
+            for v in views:
+                t = {"rgba8": torch.empty((v.height_px, v.width_px, 4), dtype=torch.uint8, device="cuda"),
+                     "flags": torch.empty((v.height_px, v.width_px), dtype=torch.int32, device="cuda"),
+                     "leaf": torch.empty((v.height_px, v.width_px, 4), dtype=torch.int32, device="cuda")}
+                o = qb.Outputs()
+                o.rgba8, o.flags, o.leaf = t["rgba8"].data_ptr(), t["flags"].data_ptr(), t["leaf"].data_ptr()
+                for k in chk:
+                    chk[k].append(t[k])
+                couts.append(o)
+            stats = ctx.render_views_ex(views, couts, True, **kw)
+            torch.cuda.synchronize()
+            frame = [{k: chk[k][i].cpu().numpy() for k in chk} for i in range(len(views))]
+            res[name] = {"mrays": rays / (statistics.mean(ms) / 1000.0) / 1e6, "ms_per_frame": statistics.mean(ms),
+                         "step_ms": [round(x, 4) for x in ms], "tuning": tuning, "frame": frame, "stats": stats}
+        ctx.set_option(lib.OPT_PERSISTENT, 1)
+        # the oracle on a seeded pixel sample, compared with every arm
+        sample = cpu_sample(scene, views, budget_s=args.proposal_cpu_seconds, seed=31,
+                            gpu_frames=res["plain_fused"]["frame"])
+        kept = sample.pop("kept")
+        for name, r in res.items():
+            n = bad8 = badf = badl = 0
+            for vi, px, py, ref in kept:
+                g = r["frame"][vi]
+                n += px.size
+                bad8 += int((g["rgba8"][py, px] != ref["rgba8"]).any(axis=-1).sum())
+                badf += int((g["flags"][py, px].view(np.uint32) != ref["flags"]).sum())
+                gl = g["leaf"][py, px]
+                # a proven pixel's shadow-leaf slot reads -2 (the plain walk's
+                # leaf was not computed); every other slot must match
+                skip = gl == -2
+                skip[:, :2] = False
+                badl += int(((gl != ref["leaf"]) & ~skip).any(axis=-1).sum())
+            r["parity_sample"] = {"pixels": n, "rgba8_mismatch": bad8, "flags_mismatch": badf,
+                                  "leaf_mismatch": badl}
+            del r["frame"]
+        two, mlp = res["plain_two_pass"]["stats"], res["learned"]["stats"]
+        vis_mlp = mlp["shadow_visits"] + mlp["proposal_visits"]
+        for r in res.values():
+            del r["stats"]
+        out["arms"] = res
+        ms_learned = res["learned"]["ms_per_frame"]
+        out.update({
+            "speedup_vs_plain_fused": res["plain_fused"]["ms_per_frame"] / ms_learned,
+            "speedup_vs_plain_two_pass": res["plain_two_pass"]["ms_per_frame"] / ms_learned,
+            "speedup_vs_plain_simple": res["plain_simple"]["ms_per_frame"] / ms_learned,
+            "persistent_speedup_vs_plain_simple": res["plain_simple"]["ms_per_frame"] / res["plain_fused"]["ms_per_frame"],
+            "shadow_rays": two["shadow_rays"], "proposals_tried": mlp["proposals_tried"],
+            "proposals_proven": mlp["proposals_proven"],
+            "hit_rate": mlp["proposals_proven"] / max(1, mlp["proposals_tried"]),
+            "shadow_visits_plain": two["shadow_visits"], "shadow_visits_learned": vis_mlp,
+            "visits_saved_frac": 1.0 - vis_mlp / max(1, two["shadow_visits"]),
+            "cpu_oracle": {k: v for k, v in sample.items() if k not in ("seconds", "rays", "parity")},
+        })
+    finally:
+        ctx.close()
+    return out
 
 
 def run_gpu(args):
@@ -557,6 +713,17 @@ def run_gpu(args):
             "visits_saved_frac": 1.0 - vis_mlp / max(1, st_two["shadow_visits"]),
         }
 
+    # the same frames on the plain one-thread-per-pixel schedule (no
+    # persistent queue, no batched ray starts), same tuning otherwise
+    ctx.set_option(qb._lib.OPT_PERSISTENT, 0)
+    simple_ms, _, _ = timed(as_graph({}) if use_graph and training is None else render_plain)
+    ctx.set_option(qb._lib.OPT_PERSISTENT, 1)
+    plain_simple = {"mrays": sum(frame_rays) / (sum(simple_ms) / 1000.0) / 1e6,
+                    "ms_per_step": statistics.mean(simple_ms),
+                    "speedup_of_value": statistics.mean(simple_ms) / statistics.mean(step_ms),
+                    "schedule": "one thread per pixel for its whole life, one warp per 32-pixel tile "
+                                "(QBC_OPT_PERSISTENT 0)"}
+
     update_ms = None
     if chars:
         # the dynamic-tree update alone (skin + rebuild + normals), untimed above
@@ -602,9 +769,13 @@ def run_gpu(args):
         "clocks": clk.summary(),
         "step_ms": [round(x, 4) for x in step_ms],
     }
+    line["plain_simple"] = plain_simple
     if proposal is not None:
         line["run"]["per_step"] = "two-pass render with occluder-network proposals (network evaluated every step)"
         line["proposal"] = proposal
+    elif not args.no_proposal_block and world == 1:
+        # the metric's learned-vs-plain comparison, on its own workload
+        line["proposal"] = proposal_comparison(args, local, stream, flush)
     line["run"]["launch"] = "CUDA graph replay (qbc_graph_launch)" if use_graph else "eager (qbc_render_views*)"
     line["run"]["tuning"] = tuning
     for g in graphs:
@@ -630,6 +801,7 @@ def run_gpu(args):
         del chk
         res = cpu_sample(scene, views, budget_s=args.cpu_seconds, character=character, frame=args.warmup,
                          gpu_frames=gpu_frames)
+        res.pop("kept", None)
         line["parity_sample"] = res.pop("parity")
         line["parity_sample"]["streams"] = "rgba8, flags, leaf (GPU frame vs the oracle on the CPU sample's pixels)"
         line["cpu_baseline"] = {k: v for k, v in res.items() if k not in ("seconds", "rays")}
@@ -662,6 +834,10 @@ def main():
     ap.add_argument("--proposal-gate", type=int, default=500, help="occlusion probability (per mille) to try")
     ap.add_argument("--proposal-level", type=int, default=8, help="octree level of the proposed cells")
     ap.add_argument("--proposal-count", type=int, default=3, help="network proposals tried per pixel (1..3)")
+    ap.add_argument("--no-proposal-block", action="store_true",
+                    help="skip the learned-vs-plain comparison on the proposal workload")
+    ap.add_argument("--proposal-cpu-seconds", type=float, default=4.0,
+                    help="oracle time for the proposal comparison's parity sample")
     args = ap.parse_args()
     global WORKLOAD
     if args.workload:

@@ -245,9 +245,13 @@ int qbc_camera_rays(qbc_ctx* ctx, const qbc_view* view, const int32_t* px, const
  * call; more is rejected with QBC_E_ARG. The counters are cleared on the
  * stream before each use. All calls share them: two calls whose work
  * overlaps on the GPU (different streams, different contexts on one device)
- * race and must be ordered by the caller. The first call on a device looks
- * up the array's device address; make that first call before any stream
- * capture. Host output pointers are rejected with QBC_E_ARG. Building leaf
+ * race and must be ordered by the caller. The first call on a context loads
+ * the render kernels' code (lazy module loading can otherwise place it in
+ * device memory during a later frame) and sets their shared-memory limit;
+ * make that first call before any stream capture. Every call looks up the
+ * array's device address with the context's device current, so the address
+ * stays right after a reset of the device's primary context. Host output
+ * pointers are rejected with QBC_E_ARG. Building leaf
  * boxes (QBC_OPT_BOX_PRUNE) allocates, so this call never builds them: it
  * prunes with the boxes an earlier allocating render built for the current
  * trees, and walks a tree changed since then unpruned (same pixels).
@@ -471,6 +475,13 @@ int qbc_synchronize(qbc_ctx* ctx);
  *   tiles the render kernels take from their queue (height 32 / width).
  *   QBC_OPT_BLOCKS_PER_SM  0 (default: as many as fit) .. 32: resident
  *   render blocks per SM of the persistent grid.
+ *   QBC_OPT_PERSISTENT  1 (default) or 0: the fused frame runs on the
+ *   persistent kernel (warps take tiles of all views from a work queue and
+ *   start new rays in batches), or, with 0, on the plain schedule: one
+ *   thread per pixel for the pixel's whole life, one warp per 32-pixel tile,
+ *   one launch of tiles_total / 4 blocks. Same pixels; the plain schedule is
+ *   the baseline the persistent kernel is measured against. Two-pass renders
+ *   always run persistent.
  */
 #define QBC_OPT_SERVICE_MIN 1
 #define QBC_OPT_PROPOSAL_GATE 2
@@ -478,6 +489,7 @@ int qbc_synchronize(qbc_ctx* ctx);
 #define QBC_OPT_BLOCKS_PER_SM 4
 #define QBC_OPT_PROPOSAL_COUNT 5
 #define QBC_OPT_BOX_PRUNE 6
+#define QBC_OPT_PERSISTENT 7
 int qbc_set_option(qbc_ctx* ctx, int option, int value);
 int qbc_get_option(qbc_ctx* ctx, int option, int* value);
 

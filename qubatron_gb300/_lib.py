@@ -253,6 +253,7 @@ OPT_TILE_WIDTH = 3
 OPT_BLOCKS_PER_SM = 4
 OPT_PROPOSAL_COUNT = 5
 OPT_BOX_PRUNE = 6
+OPT_PERSISTENT = 7
 
 
 def lib_path() -> str:

@@ -33,6 +33,7 @@ struct FrameSignature {
   int32_t tile_shift;
   int32_t blocks_per_sm;
   int32_t proposal_count;
+  int32_t persistent;
 };
 
 bool same_signature(const FrameSignature& a, const FrameSignature& b) {
@@ -46,7 +47,7 @@ bool same_signature(const FrameSignature& a, const FrameSignature& b) {
   return a.rec == b.rec && a.rec_cap == b.rec_cap && a.pixlog == b.pixlog && a.pixlog_cap == b.pixlog_cap &&
          a.net_w == b.net_w && a.net_b == b.net_b && a.stream == b.stream && a.service_min == b.service_min &&
          a.proposal_gate == b.proposal_gate && a.tile_shift == b.tile_shift && a.blocks_per_sm == b.blocks_per_sm &&
-         a.proposal_count == b.proposal_count;
+         a.proposal_count == b.proposal_count && a.persistent == b.persistent;
 }
 
 FrameSignature frame_signature(const qbc_ctx* c) {
@@ -64,6 +65,7 @@ FrameSignature frame_signature(const qbc_ctx* c) {
   f.tile_shift = c->tile_shift;
   f.blocks_per_sm = c->blocks_per_sm;
   f.proposal_count = c->proposal_count;
+  f.persistent = c->persistent;
   return f;
 }
 

@@ -67,13 +67,14 @@ struct qbc_ctx {
   bool fused_attr[2] = {false, false};  // dynamic shared memory set for the fused network kernels
   std::vector<qbc_graph*> graphs;       // captured frames, detached when the context goes
   int render_blocks[4] = {0, 0, 0, 0};  // resident blocks per SM of each render_kernel variant
-  int attr_done = 0;
+  uint64_t attr_done = 0;  // kernel variants whose shared-memory limit is set (bit per variant)
   int service_min = qbc::kServiceMinDefault;
   int tile_shift = 3;     // 8x4 warp tiles
   int blocks_per_sm = 0;  // render blocks per SM (0: as many as fit)
   int proposal_gate = 500;  // per mille: minimum predicted occlusion probability to try a proposal
   int proposal_count = 3;   // network proposals tried per pixel (earliest first)
   int box_prune = 1;        // skip subtrees whose leaf boxes the ray misses
+  int persistent = 1;       // fused frames on the persistent kernel (0: one thread per pixel)
   int64_t launches = 0;
 };
 

@@ -11,7 +11,6 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
-#include <mutex>
 #include <memory>
 #include <new>
 #include <vector>
@@ -140,6 +139,11 @@ extern "C" int qbc_set_option(qbc_ctx* c, int option, int value) {
     c->blocks_per_sm = value;
     return QBC_OK;
   }
+  if (option == QBC_OPT_PERSISTENT) {
+    if (value < 0 || value > 1) return fail(QBC_E_ARG, "qbc_set_option: persistent %d (0 or 1)", value);
+    c->persistent = value;
+    return QBC_OK;
+  }
   return fail(QBC_E_ARG, "qbc_set_option: unknown option %d", option);
 }
 
@@ -167,6 +171,10 @@ extern "C" int qbc_get_option(qbc_ctx* c, int option, int* value) {
   }
   if (option == QBC_OPT_BLOCKS_PER_SM) {
     *value = c->blocks_per_sm;
+    return QBC_OK;
+  }
+  if (option == QBC_OPT_PERSISTENT) {
+    *value = c->persistent;
     return QBC_OK;
   }
   return fail(QBC_E_ARG, "qbc_get_option: unknown option %d", option);
@@ -685,9 +693,9 @@ template <bool EXACT, bool DYN, int MODE, bool PROP>
 int launch_render(qbc_ctx* c, const qbc::Batch& b, size_t smem, const qbc::Wave& wave) {
   auto kern = qbc::render_kernel<EXACT, DYN, MODE, PROP>;
   const int variant = (EXACT ? 1 : 0) + (DYN ? 2 : 0) + 4 * MODE + (PROP ? 16 : 0);
-  if (!(c->attr_done & (1 << variant))) {
+  if (!(c->attr_done & (1ull << variant))) {
     QBC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-    c->attr_done |= 1 << variant;
+    c->attr_done |= 1ull << variant;
   }
   int per_sm = 0;
   QBC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, qbc::kThreads, smem));
@@ -708,8 +716,28 @@ int launch_render(qbc_ctx* c, const qbc::Batch& b, size_t smem, const qbc::Wave&
   return QBC_OK;
 }
 
+// The plain schedule: one warp per 32-pixel tile, 4 tiles per block.
+template <bool EXACT, bool DYN>
+int launch_simple(qbc_ctx* c, const qbc::Batch& b, size_t smem) {
+  auto kern = qbc::simple_kernel<EXACT, DYN>;
+  const int variant = 32 + (EXACT ? 1 : 0) + (DYN ? 2 : 0);
+  if (!(c->attr_done & (1ull << variant))) {
+    QBC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+    c->attr_done |= 1ull << variant;
+  }
+  const int64_t blocks = std::max<int64_t>(1, ((int64_t)b.tiles_total + 3) / 4);
+  qbc::DevScene sc = device_scene(c);
+  for (int i = 0; i < b.n; ++i)
+    if (b.job[i].o.visits) sc.box_words = c->wstats + qbc::kStatBoxWords;
+  kern<<<(unsigned)blocks, qbc::kThreads, smem, c->stream>>>(sc, b);
+  QBC_CUDA(cudaGetLastError());
+  ++c->launches;
+  return QBC_OK;
+}
+
 template <bool EXACT, bool DYN>
 int launch_modes(qbc_ctx* c, const qbc::Batch& b, size_t smem, const qbc_render_opts* opts, int64_t pixels) {
+  if ((!opts || !opts->two_pass) && !c->persistent) return launch_simple<EXACT, DYN>(c, b, smem);
   if (!opts || !opts->two_pass) return launch_render<EXACT, DYN, qbc::kFused, false>(c, b, smem, qbc::Wave{});
   // two passes: primary rays -> record queue -> shade pass
   if (c->rec_cap < pixels) {
@@ -1038,35 +1066,49 @@ extern "C" int qbc_camera_rays(qbc_ctx* c, const qbc_view* view, const int32_t* 
 
 // Work-queue counters of qbc_render_views_noalloc: one per launch of 32
 // views. File-scope static device memory, so the call needs no allocation;
-// every GPU that loads the library holds these 256 bytes until exit.
+// every GPU that loads the library holds these 32 bytes until exit.
 static __device__ __align__(256) unsigned int qbc_noalloc_queues[QBC_NOALLOC_MAX_LAUNCHES];
+static_assert(QBC_NOALLOC_MAX_VIEWS <= QBC_NOALLOC_MAX_LAUNCHES * qbc::kMaxViewsPerLaunch,
+              "every launch of a maximal no-allocation call needs its own counter");
 
 namespace {
 
-constexpr int kNoallocMaxDevices = 64;
-std::mutex g_noalloc_mu;
-unsigned int* g_noalloc_ptr[kNoallocMaxDevices] = {};
-
-// Device address of the counters on the current device, looked up once per
-// device (cudaGetSymbolAddress with that device current).
-int noalloc_queues(int device, unsigned int** out) {
-  if (device < 0 || device >= kNoallocMaxDevices)
-    return fail(QBC_E_ARG, "qbc_render_views_noalloc: device %d beyond %d", device, kNoallocMaxDevices);
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[device]) {
-    void* ptr = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&ptr, qbc_noalloc_queues);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(qbc_noalloc_queues)");
-    g_noalloc_ptr[device] = static_cast<unsigned int*>(ptr);
+// Shared-memory limit of a fused render_kernel variant, set once per context
+// (the same per-context cache launch_render uses). Setting it also loads the
+// kernel's code under lazy module loading.
+template <bool EXACT, bool DYN>
+int fused_attr(qbc_ctx* c) {
+  const int variant = (EXACT ? 1 : 0) + (DYN ? 2 : 0);
+  if (!(c->attr_done & (1ull << variant))) {
+    QBC_CUDA(cudaFuncSetAttribute(qbc::render_kernel<EXACT, DYN, qbc::kFused, false>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+    c->attr_done |= 1ull << variant;
   }
-  *out = g_noalloc_ptr[device];
+  return QBC_OK;
+}
+
+// Set-up of a no-allocation render on the context's device (current): the
+// four fused kernel variants are loaded and given their shared-memory limit
+// (on the context's first call; loading code can take device memory, so it
+// happens here and not in a later frame), and the counters' device address
+// is looked up with that device current. The lookup runs on every call, so
+// an address never outlives the primary context it came from.
+int noalloc_setup(qbc_ctx* c, unsigned int** out) {
+  int rc = fused_attr<true, true>(c);
+  if (!rc) rc = fused_attr<true, false>(c);
+  if (!rc) rc = fused_attr<false, true>(c);
+  if (!rc) rc = fused_attr<false, false>(c);
+  if (rc) return rc;
+  void* ptr = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&ptr, qbc_noalloc_queues);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(qbc_noalloc_queues)");
+  *out = static_cast<unsigned int*>(ptr);
   return QBC_OK;
 }
 
 template <bool EXACT, bool DYN>
 int launch_render_noalloc(qbc_ctx* c, const qbc::Batch& b, size_t smem, unsigned int* queue) {
   auto kern = qbc::render_kernel<EXACT, DYN, qbc::kFused, false>;
-  QBC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
   int per_sm = 0;
   QBC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, qbc::kThreads, smem));
   if (per_sm < 1) return fail(QBC_E_STATE, "render_kernel: no block fits on an SM with %zu B shared memory", smem);
@@ -1107,9 +1149,12 @@ extern "C" int qbc_render_views_noalloc(qbc_ctx* c, const qbc_view* views, const
     }
   }
   unsigned int* queues = nullptr;
-  int rc = noalloc_queues(c->device, &queues);
+  int rc = noalloc_setup(c, &queues);
   if (rc) return rc;
   const int launches = (n + qbc::kMaxViewsPerLaunch - 1) / qbc::kMaxViewsPerLaunch;
+  if (launches > QBC_NOALLOC_MAX_LAUNCHES)
+    return fail(QBC_E_ARG, "qbc_render_views_noalloc: %d launches exceed the %d counters", launches,
+                QBC_NOALLOC_MAX_LAUNCHES);
   // the counters keep the previous call's values: start every used one at 0
   QBC_CUDA(cudaMemsetAsync(queues, 0, sizeof(unsigned int) * (size_t)launches, c->stream));
   const bool dyn = c->tree[1].n > 0;

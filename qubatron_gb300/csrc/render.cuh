@@ -627,6 +627,51 @@ __global__ void __launch_bounds__(kThreads, render_min_blocks<EXACT, DYN, MODE>(
   }
 }
 
+// The plain schedule (QBC_OPT_PERSISTENT 0): one thread per pixel for its
+// whole life (primary ray, shadow ray, shading, flare), one warp per 32-pixel
+// tile, no work queue and no batched service; a lane whose pixel is done
+// idles until its warp's last pixel is. Same walker and shader code as
+// render_kernel, so the same pixels; kept as the baseline the persistent
+// kernel is measured against.
+template <bool EXACT, bool DYN>
+__global__ void __launch_bounds__(kThreads, render_min_blocks<EXACT, DYN, kFused>()) simple_kernel(DevScene sc, const __grid_constant__ Batch batch) {
+  extern __shared__ uint32_t smem[];
+  const int tid = threadIdx.x;
+  const int tile = (int)((blockIdx.x * (unsigned)kThreads + tid) >> 5);
+  if (tile >= batch.tiles_total) return;
+  constexpr int kW = Walker<EXACT, DYN, false>::kWords;
+  const Wave wave{};
+  Shader<EXACT, DYN, kFused, false> S{sc, batch, wave, Stack{smem + tid, kThreads},
+                                      PixRef{smem + kW * batch.max_level * kThreads + tid}};
+  S.running = false;
+  S.enqueue = false;
+  S.prop_k = 0;
+  S.rec_q = 0;
+  S.next_target = 0;
+  S.next_tdepth = 0;
+  const int vi = tile_view(batch, tile);
+  const ViewJob& J = batch.job[vi];
+  const int t = tile - J.tile_begin, slot = tid & 31, sh = batch.tile_shift;
+  const int x = ((t % J.tiles_x) << sh) + (slot & ((1 << sh) - 1));
+  const int y = (t / J.tiles_x) * (32 >> sh) + (slot >> sh);
+  if (x >= J.v.width_px || y >= J.v.height_px) return;
+  float3 rp, rd;
+  S.begin_pixel(vi, x, y, rp, rd);
+  for (;;) {
+    if (S.w.start(S.bc, rp, rd, sc, S.maxlevel) == kDiscard) {
+      S.discard();
+      return;
+    }
+    const bool fast = EXACT && (S.w.mode & 1u);
+    int r;
+    do {
+      r = S.w.step(sc, S.maxlevel, S.bc, S.st, fast);
+    } while (r == kRunning);
+    S.result = r;
+    if (!S.consume(rp, rd)) return;
+  }
+}
+
 struct RayJob {
   const float* pos;
   const float* dir;

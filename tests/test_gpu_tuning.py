@@ -87,3 +87,35 @@ def test_autotune(ctx, floor50k_scene):
             ctx.set_option(opt, bad)
     with pytest.raises(QbcError):
         ctx.autotune(views, outs, reps=0)
+
+
+@pytest.mark.parametrize("dynamic", [False, True])
+def test_plain_schedule_renders_the_same_pixels(ctx, floor50k_scene, dynamic):
+    """QBC_OPT_PERSISTENT 0 (one thread per pixel, no work queue) renders
+    every stream, visit counts included, exactly as the persistent kernel,
+    with one tree and with two, and against the oracle."""
+    import qubatron_gb300._lib as L
+    from qubatron_gb300 import scenes
+    from oracle import qbo
+    from helpers import compare_frame
+    s = floor50k_scene
+    d = (None, None, None)
+    if dynamic:
+        ch = scenes.make_character(20_000, root=(850.0, 430.0, 1250.0))
+        d = (scenes.build_octree(ch.rest_points, S, LEVELS), ch.colors, ch.rest_normals)
+    upload_scene(ctx, s.nodes, s.colors, s.normals, *d)
+    views = _views()
+    ref = ctx.render_host(views, ALL)
+    for tw in (4, 8, 32):
+        ctx.set_option(L.OPT_TILE_WIDTH, tw)
+        ctx.set_option(L.OPT_PERSISTENT, 0)
+        got = ctx.render_host(views, ALL)
+        _same(ref, got, f"plain schedule, tile {tw}")
+        ctx.set_option(L.OPT_PERSISTENT, 1)
+    ctx.set_option(L.OPT_BOX_PRUNE, 0)
+    ctx.set_option(L.OPT_PERSISTENT, 0)
+    sc = qbo.Scene(s.nodes, s.colors, s.normals, *d)
+    for v, g in zip(views, ctx.render_host(views, ALL)):
+        compare_frame(g.arrays, qbo.render(sc, qbo.QboView.from_bytes(v.to_bytes())), "plain schedule", visits=True)
+    with pytest.raises(Exception):
+        ctx.set_option(L.OPT_PERSISTENT, 2)

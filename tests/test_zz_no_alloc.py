@@ -111,3 +111,45 @@ def test_noalloc_rejects_too_many_views_and_host_outputs(floor50k_scene):
         ctx.synchronize()
     finally:
         ctx.close()
+
+
+def test_noalloc_two_trees_without_a_render_first(floor50k_scene):
+    """Both trees uploaded and no allocating render since: the call takes the
+    two-tree kernel, walks without leaf boxes (none were built for these
+    trees) and must equal qbc_render_views with pruning off on every stream,
+    visit counts included; around its later calls the device's free memory
+    does not move."""
+    torch = pytest.importorskip("torch")
+    import qubatron_gb300 as qb
+    from qubatron_gb300 import scenes
+    s = floor50k_scene
+    ch = scenes.make_character(30_000, root=(620.0, 460.0, 1150.0))
+    d_nodes = scenes.build_octree(ch.rest_points, S, LEVELS)
+    ctx = qb.OctreeGLC(0)
+    try:
+        upload_scene(ctx, s.nodes, s.colors, s.normals, d_nodes, ch.colors, ch.rest_normals)
+        views = _views()
+        got = []
+        for call in range(3):
+            bufs, outs = _device_outputs(torch, views, 5 + call)
+            free0 = torch.cuda.mem_get_info()[0]
+            ctx.render_views_noalloc(views, outs)
+            ctx.synchronize()
+            if call > 0:  # the first call may load the kernels' code
+                assert torch.cuda.mem_get_info()[0] == free0, f"call {call} changed the device's free memory"
+            got.append(_host(bufs))
+        ctx.set_option(qb._lib.OPT_BOX_PRUNE, 0)
+        ref_bufs, ref_outs = _device_outputs(torch, views, 0)
+        ctx.render_views(views, ref_outs, on_device=True)
+        ctx.synchronize()
+        ref = _host(ref_bufs)
+        assert sum(int(r["visits"][..., 1].sum()) for r in ref) > 0, "no view walked the dynamic tree"
+        for call, g_all in enumerate(got):
+            for vi, (g, r) in enumerate(zip(g_all, ref)):
+                for name, _, _ in STREAMS:
+                    a, b = g[name], r[name]
+                    if a.dtype == np.float32:
+                        a, b = a.view(np.uint32), b.view(np.uint32)
+                    assert np.array_equal(a, b), f"call {call}, view {vi}, stream {name}"
+    finally:
+        ctx.close()
