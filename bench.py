@@ -191,35 +191,42 @@ def prepare(workload_name: str, host_nodes: bool = True):
 
 
 class CharacterFrames:
-    """The dynamic basecube of a frame: skin the character on the GPU for the
-    frame's bone pose, rebuild the dynamic tree from the skinned points and
-    take the skinned normals, all on the device (qbc_skin_rigid,
-    qbc_build_tree, qbc_upload_device)."""
+    """The dynamic basecube of a frame, on the device: the frame's bone set
+    (pinned on the host for every frame, copied on the stream) is written
+    into a device buffer that qbc_dynamic_update_run reads; it re-skins the
+    character, rebuilds the dynamic tree and takes the skinned normals, with
+    no allocation and no host round trip, so the whole frame can also be
+    captured as one graph (qbc_graph_capture_dynamic)."""
 
-    def __init__(self, ctx, ch):
+    def __init__(self, ctx, ch, n_frames: int):
         import torch
         import qubatron_gb300 as qb
+        from qubatron_gb300 import scenes
         self.qb, self.ctx, self.ch = qb, ctx, ch
         self.n = ch.rest_points.shape[0]
+        self.n_bones = ch.joints.shape[0] - 1
         self.rp = torch.from_numpy(ch.rest_points).cuda()
         self.rn = torch.from_numpy(ch.rest_normals).cuda()
         self.bone = torch.from_numpy(ch.bone).cuda()
         self.op = torch.empty_like(self.rp)
         self.on = torch.empty_like(self.rn)
+        self.bones_dev = torch.zeros((self.n_bones, 12), dtype=torch.float32, device="cuda")
+        self.host = [torch.from_numpy(scenes.pose_bones(ch, f)).pin_memory() for f in range(n_frames)]
+        self.h2d_bytes = self.n_bones * 12 * 4
+        self.update = qb._lib.DynamicUpdate(self.rp.data_ptr(), self.rn.data_ptr(), self.bone.data_ptr(),
+                                            self.bones_dev.data_ptr(), self.op.data_ptr(), self.on.data_ptr(), self.n,
+                                            self.n_bones, 12, 1800.0, 0)
         col = np.ascontiguousarray(ch.colors)
         ctx.upload_texbuffer_data(col, qb.GL_FLOAT, col.nbytes, 12, 0, col.nbytes, qb.OCTREE_GLC_BUFFER_DYNAMIC_COLOR)
         torch.cuda.synchronize()
 
-    def bones(self, frame):
-        from qubatron_gb300 import scenes
-        return scenes.pose_bones(self.ch, frame)
+    def set_bones(self, frame: int):
+        self.bones_dev.copy_(self.host[frame], non_blocking=True)
 
-    def apply(self, bones):
-        qb, ctx, n = self.qb, self.ctx, self.n
-        ctx.skin_rigid(self.rp.data_ptr(), self.rn.data_ptr(), self.bone.data_ptr(), n, bones, self.op.data_ptr(),
-                       self.on.data_ptr())
-        ctx.build_tree(True, (self.op.data_ptr(), n), 1800.0, 12)
-        ctx.upload_device(self.on.data_ptr(), qb.GL_FLOAT, n * 12, 12, 0, n * 12, qb.OCTREE_GLC_BUFFER_DYNAMIC_NORMAL)
+    def apply(self, frame: int):
+        """Bones of `frame`, then the update, queued on the stream."""
+        self.set_bones(frame)
+        self.ctx.dynamic_update(self.update)
 
 
 def count_rays(flags: np.ndarray) -> int:
@@ -329,7 +336,7 @@ def run_reference(args):
     return 0
 
 
-def measure_e2e(ctx, views, rays, world, flush, steps, update=None, render=None):
+def measure_e2e(ctx, views, rays, world, flush, steps, update=None, render=None, h2d_extra=0):
     """Same views through the public C ABI into pinned host buffers: the
     timed call includes the kernel and the copy of every frame to the host."""
     render = render or (lambda v, o, dev: ctx.render_views(v, o, on_device=dev))
@@ -355,7 +362,7 @@ def measure_e2e(ctx, views, rays, world, flush, steps, update=None, render=None)
     from qubatron_gb300 import replicas
     rate, slowest_s = replicas.job_throughput(rays * len(e2e_t), sum(e2e_t), device="cuda")
     d2h = sum(h.numel() for h in host)
-    h2d = len(views) * 132  # qbc_view uniforms, passed as launch parameters
+    h2d = len(views) * 132 + h2d_extra  # qbc_view uniforms (launch parameters), bone sets
     return {"value": rate / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h, "ms_per_step": 1000.0 * slowest_s / len(e2e_t)}
 
@@ -563,15 +570,37 @@ def run_gpu(args):
     graphs = []
 
     def as_graph(kw):
-        """The frame as a CUDA graph (static scenes): each step is one
-        qbc_graph_launch into the device outputs."""
-        g = ctx.graph_capture(views, outs, **kw)
+        """The frame as a CUDA graph: each step is one qbc_graph_launch into
+        the device outputs; with a character the graph also holds the
+        frame's dynamic update (skin, rebuild, normals), and a step writes
+        the frame's bones before the launch."""
+        g = ctx.graph_capture_dynamic(chars.update, views, outs, **kw) if chars else ctx.graph_capture(views, outs, **kw)
         graphs.append(g)
-        return lambda v, o, dev: g.launch()
+        fn = lambda v, o, dev: g.launch()  # noqa: E731
+        fn.graph = True
+        return fn
+
+    # device outputs
+    frames = [torch.empty((v.height_px, v.width_px, 4), dtype=torch.uint8, device="cuda") for v in views]
+    outs = []
+    for f in frames:
+        o = qb.Outputs()
+        o.rgba8 = f.data_ptr()
+        outs.append(o)
+
+    n_frames = args.warmup + args.steps
+    chars = CharacterFrames(ctx, character, n_frames) if character is not None else None
+
+    def update(frame, eager=True):
+        """The frame's dynamic basecube: the whole update, or (graph steps)
+        only its bones."""
+        if chars:
+            chars.apply(frame) if eager else chars.set_bones(frame)
 
     render = render_plain
     training = None
     if w.train_poses:
+        update(0)
         # occluder-proposal network: log the plain shadow walks of the
         # training poses, train on them (both untimed), render the held-out
         # poses with its proposals
@@ -595,22 +624,6 @@ def run_gpu(args):
         training["proposal_count"] = args.proposal_count
         render = render_mlp
 
-    # device outputs
-    frames = [torch.empty((v.height_px, v.width_px, 4), dtype=torch.uint8, device="cuda") for v in views]
-    outs = []
-    for f in frames:
-        o = qb.Outputs()
-        o.rgba8 = f.data_ptr()
-        outs.append(o)
-
-    chars = CharacterFrames(ctx, character) if character is not None else None
-    n_frames = args.warmup + args.steps
-    poses = [chars.bones(f) for f in range(n_frames)] if chars else [None] * n_frames
-
-    def update(frame):
-        if chars:
-            chars.apply(poses[frame])
-
     tuning = None
     if args.autotune and not (args.service_min or args.tile_width or args.blocks_per_sm):
         # tuning options (service threshold, warp tile, blocks per SM) picked
@@ -622,7 +635,7 @@ def run_gpu(args):
         tuning["views_timed"] = k
         torch.cuda.synchronize()
 
-    use_graph = args.graph and chars is None
+    use_graph = args.graph
     if use_graph:
         render = as_graph(mlp_kw if training is not None else {})
 
@@ -664,8 +677,9 @@ def run_gpu(args):
     flush = torch.empty(2 * L2_BYTES, dtype=torch.uint8, device="cuda")
 
     def timed(render_fn):
+        eager = not getattr(render_fn, "graph", False)
         for f in range(args.warmup):
-            update(f)
+            update(f, eager)
             render_fn(views, outs, True)
         torch.cuda.synchronize()
         l0 = ctx.launch_count()
@@ -676,7 +690,7 @@ def run_gpu(args):
             for k in range(args.steps):
                 flush.zero_()
                 ev[k][0].record(stream)
-                update(args.warmup + k)
+                update(args.warmup + k, eager)
                 render_fn(views, outs, True)
                 ev[k][1].record(stream)
             torch.cuda.synchronize()
@@ -716,7 +730,7 @@ def run_gpu(args):
     # the same frames on the plain one-thread-per-pixel schedule (no
     # persistent queue, no batched ray starts), same tuning otherwise
     ctx.set_option(qb._lib.OPT_PERSISTENT, 0)
-    simple_ms, _, _ = timed(as_graph({}) if use_graph and training is None else render_plain)
+    simple_ms, _, _ = timed(as_graph({}) if use_graph else render_plain)
     ctx.set_option(qb._lib.OPT_PERSISTENT, 1)
     plain_simple = {"mrays": sum(frame_rays) / (sum(simple_ms) / 1000.0) / 1e6,
                     "ms_per_step": statistics.mean(simple_ms),
@@ -739,7 +753,8 @@ def run_gpu(args):
     if not args.no_e2e:
         e2e = measure_e2e(ctx, views, rays, world, flush, args.steps,
                           (lambda k: update(args.warmup + k % args.steps)) if chars else None,
-                          render_mlp if training is not None else render_plain)
+                          render_mlp if training is not None else render_plain,
+                          chars.h2d_bytes if chars else 0)
 
     hbm, peak_kind = peaks()
 

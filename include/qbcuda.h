@@ -164,6 +164,41 @@ int qbc_upload_device(qbc_ctx* ctx, const void* data, int type, size_t size, siz
 int qbc_skin_rigid(qbc_ctx* ctx, const float* rest_pnts, const float* rest_nrms, const int32_t* bone, int64_t n, const float* bones, int n_bones, float* out_pnts, float* out_nrms);
 
 /*
+ * The per-frame update of the dynamic basecube as one call: rigid skinning
+ * of the rest points with the bone set in DEVICE memory (read when the work
+ * runs), the dynamic tree rebuilt on the GPU from the skinned points
+ * (octree_reset + octree_insert_point in point order, octree.c:89-147, model
+ * indices 0..n-1), and the skinned normals taken as the dynamic model's
+ * normals. The reference does this on the host each frame, reading the
+ * skinned paths back from its skeleton shader and uploading the dynamic
+ * octree and normals again (qubatron.c:439-452, 508-529; skeleton_glc.c:238-245).
+ * All arrays are device memory of the context's GPU; pnts / nrms receive the
+ * skinned points and normals. The call queues the work on the context's
+ * stream and returns: no host synchronisation, and no allocation once the
+ * buffers have this update's size (the first call of a size allocates). A
+ * bone index outside the set skins with bone 0; a skinned point that is
+ * negative or not finite is left out of the tree; either is reported by the
+ * next qbc_synchronize / qbc_tree_nodes / qbc_download_tree. The colours of
+ * the dynamic model are uploaded once, as the reference does.
+ */
+typedef struct qbc_dynamic_update
+{
+    const float*   rest_pnts; /* n float3 */
+    const float*   rest_nrms; /* n float3, or NULL (then nrms NULL) */
+    const int32_t* bone;      /* n bone indices */
+    const float*   bones;     /* n_bones x 12 floats: R row-major, t; p' = R p + t */
+    float*         pnts;      /* n float3 out */
+    float*         nrms;      /* n float3 out, or NULL */
+    int64_t        n;
+    int32_t        n_bones;   /* 1..QBC_MAX_BONES */
+    int32_t        levels;    /* tree depth, 0..21 */
+    float          basesize;  /* basecube edge of the dynamic tree */
+    int32_t        pad;
+} qbc_dynamic_update;
+
+int qbc_dynamic_update_run(qbc_ctx* ctx, const qbc_dynamic_update* update);
+
+/*
  * Derive the uniforms of one frame from the arguments of octree_glc_update
  * (octree_glc.c:249-284). focal <= 0 selects the reference's focal length
  * (ow/2)/tan(pi/4) (octree_fsh.c:403); a positive value sets cfp.z directly.
@@ -398,6 +433,17 @@ int qbc_autotune(qbc_ctx* ctx, const qbc_view* views, const qbc_outputs* dev_out
  */
 typedef struct qbc_graph qbc_graph;
 int qbc_graph_capture(qbc_ctx* ctx, const qbc_view* views, const qbc_outputs* dev_outs, int n, const qbc_render_opts* opts, qbc_graph** graph);
+/*
+ * The same with the frame's dynamic update captured in front of the render
+ * (qbc_dynamic_update_run: skin with the bones in device memory, rebuild the
+ * dynamic tree, take the normals): one replay then re-skins, rebuilds and
+ * renders, with no host round trip. Write the next frame's bones into
+ * update->bones (on the context's stream, or before the launch) and call
+ * qbc_graph_launch. The update's arrays and sizes are held by the graph; the
+ * dynamic tree's buffers are sized for the update's node bound, so replays
+ * never reallocate. qbc_graph_update re-captures both parts.
+ */
+int qbc_graph_capture_dynamic(qbc_ctx* ctx, const qbc_dynamic_update* update, const qbc_view* views, const qbc_outputs* dev_outs, int n, const qbc_render_opts* opts, qbc_graph** graph);
 int qbc_graph_update(qbc_graph* graph, const qbc_view* views, int n);
 int qbc_graph_launch(qbc_graph* graph);
 int qbc_graph_destroy(qbc_graph* graph);

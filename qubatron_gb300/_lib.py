@@ -113,6 +113,24 @@ class RenderOpts(C.Structure):
     ]
 
 
+class DynamicUpdate(C.Structure):
+    """qbc_dynamic_update: device pointers of one per-frame dynamic update."""
+
+    _fields_ = [
+        ("rest_pnts", C.c_void_p),
+        ("rest_nrms", C.c_void_p),
+        ("bone", C.c_void_p),
+        ("bones", C.c_void_p),
+        ("pnts", C.c_void_p),
+        ("nrms", C.c_void_p),
+        ("n", C.c_int64),
+        ("n_bones", C.c_int32),
+        ("levels", C.c_int32),
+        ("basesize", C.c_float),
+        ("pad", C.c_int32),
+    ]
+
+
 class RenderStats(C.Structure):
     """qbc_render_stats."""
 
@@ -213,6 +231,10 @@ SIGNATURES = {
                                C.POINTER(TuneResult)]),
     "qbc_graph_capture": (C.c_int, [C.c_void_p, C.POINTER(View), C.POINTER(Outputs), C.c_int, C.POINTER(RenderOpts),
                                     C.POINTER(C.c_void_p)]),
+    "qbc_graph_capture_dynamic": (C.c_int, [C.c_void_p, C.POINTER(DynamicUpdate), C.POINTER(View),
+                                            C.POINTER(Outputs), C.c_int, C.POINTER(RenderOpts),
+                                            C.POINTER(C.c_void_p)]),
+    "qbc_dynamic_update_run": (C.c_int, [C.c_void_p, C.POINTER(DynamicUpdate)]),
     "qbc_graph_update": (C.c_int, [C.c_void_p, C.POINTER(View), C.c_int]),
     "qbc_graph_launch": (C.c_int, [C.c_void_p]),
     "qbc_graph_destroy": (C.c_int, [C.c_void_p]),

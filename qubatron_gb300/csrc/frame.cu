@@ -83,6 +83,8 @@ struct qbc_graph {
   int n = 0;
   int64_t kernels = 0;
   FrameSignature sig;
+  qbc_dynamic_update update;  // captured in front of the render when has_update
+  bool has_update = false;
 };
 
 namespace {
@@ -90,7 +92,8 @@ namespace {
 int capture_frame(qbc_graph* g, const qbc_view* views, cudaGraph_t* out) {
   qbc_ctx* c = g->ctx;
   QBC_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-  const int rc = render_views_impl(c, views, g->outs.data(), g->n, 1, g->has_opts ? &g->opts : nullptr, nullptr);
+  int rc = g->has_update ? dynamic_update(c, &g->update) : QBC_OK;
+  if (!rc) rc = render_views_impl(c, views, g->outs.data(), g->n, 1, g->has_opts ? &g->opts : nullptr, nullptr);
   cudaGraph_t graph = nullptr;
   const cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
   if (rc || e != cudaSuccess) {
@@ -131,19 +134,25 @@ void detach_graph(qbc_graph* g) {
   g->ctx = nullptr;
 }
 
-extern "C" int qbc_graph_capture(qbc_ctx* c, const qbc_view* views, const qbc_outputs* dev_outs, int n,
-                                 const qbc_render_opts* opts, qbc_graph** out) {
-  qbc::clear_error();
+namespace {
+
+int capture_impl(qbc_ctx* c, const qbc_dynamic_update* update, const qbc_view* views, const qbc_outputs* dev_outs,
+                 int n, const qbc_render_opts* opts, qbc_graph** out) {
   if (!c || !views || !dev_outs || !out || n <= 0) return fail(QBC_E_ARG, "qbc_graph_capture: bad argument");
   int rc = check_render_opts(opts, n);
   if (rc) return rc;
   QBC_CUDA(cudaSetDevice(c->device));
   // one eager frame first: buffers grown and kernel attributes set before
   // the capture, which must not allocate
-  rc = render_views_impl(c, views, dev_outs, n, 1, opts, nullptr);
+  if (update) rc = dynamic_update(c, update);
+  if (!rc) rc = render_views_impl(c, views, dev_outs, n, 1, opts, nullptr);
   if (rc) return rc;
   QBC_CUDA(cudaStreamSynchronize(c->stream));
   std::unique_ptr<qbc_graph> g(new qbc_graph());
+  if (update) {
+    g->update = *update;
+    g->has_update = true;
+  }
   g->ctx = c;
   g->n = n;
   g->outs.assign(dev_outs, dev_outs + n);
@@ -168,6 +177,22 @@ extern "C" int qbc_graph_capture(qbc_ctx* c, const qbc_view* views, const qbc_ou
   c->graphs.push_back(g.get());
   *out = g.release();
   return QBC_OK;
+}
+
+}  // namespace
+
+extern "C" int qbc_graph_capture(qbc_ctx* c, const qbc_view* views, const qbc_outputs* dev_outs, int n,
+                                 const qbc_render_opts* opts, qbc_graph** out) {
+  qbc::clear_error();
+  return capture_impl(c, nullptr, views, dev_outs, n, opts, out);
+}
+
+extern "C" int qbc_graph_capture_dynamic(qbc_ctx* c, const qbc_dynamic_update* update, const qbc_view* views,
+                                         const qbc_outputs* dev_outs, int n, const qbc_render_opts* opts,
+                                         qbc_graph** out) {
+  qbc::clear_error();
+  if (!update) return fail(QBC_E_ARG, "qbc_graph_capture_dynamic: null update");
+  return capture_impl(c, update, views, dev_outs, n, opts, out);
 }
 
 extern "C" int qbc_graph_update(qbc_graph* g, const qbc_view* views, int n) {

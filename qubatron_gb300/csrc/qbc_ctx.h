@@ -28,6 +28,10 @@ struct DevTreeBuf {
   int64_t cbox_cap = 0;  // nodes
   int box_depth = -1;
   bool box_valid = false;
+  // a GPU build leaves the exact node count on the device (d_count) and n at
+  // the build's bound; the count is read back only when the host asks
+  bool count_on_device = false;
+  int32_t* d_count = nullptr;
 };
 
 struct DevModelBuf {
@@ -76,7 +80,22 @@ struct qbc_ctx {
   int box_prune = 1;        // skip subtrees whose leaf boxes the ray misses
   int persistent = 1;       // fused frames on the persistent kernel (0: one thread per pixel)
   int64_t launches = 0;
+  qbc::BuildScratch build;       // GPU tree build scratch, kept for per-frame rebuilds
+  void* build_input = nullptr;   // device copy of host build input
+  int64_t build_input_cap = 0;   // bytes
+  unsigned* derr = nullptr;      // device: qbc::DeviceError bits of kernels' input checks
+  int32_t* counts = nullptr;     // device: node counts of GPU-built trees (one per tree)
 };
+
+// Node count of a tree; a GPU-built tree's count is read from the device
+// (synchronizes).
+int tree_count(qbc_ctx* c, int tree, int64_t* n);
+// Report and clear the device-side input faults recorded since the last
+// check (synchronizes).
+int check_device_errors(qbc_ctx* c);
+// Enqueue a per-frame dynamic update (skin, rebuild, normals); no allocation
+// once the buffers have the update's size, no host synchronisation.
+int dynamic_update(qbc_ctx* c, const qbc_dynamic_update* u);
 
 constexpr size_t kStageMax = size_t(256) << 20;
 

@@ -61,12 +61,17 @@ extern "C" int qbc_create(int device, qbc_ctx** out) {
   if (e == cudaSuccess) e = cudaMalloc(&c->queue, sizeof(unsigned int));
   if (e == cudaSuccess) e = cudaMalloc(&c->wcount, 2 * sizeof(unsigned int));
   if (e == cudaSuccess) e = cudaMalloc(&c->wstats, qbc::kStatCount * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&c->derr, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemset(c->derr, 0, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMalloc(&c->counts, 2 * sizeof(int32_t));
   if (e != cudaSuccess) {
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
     return cuda_fail(e, "qbc_create");
   }
   c->stream = c->own;
+  c->tree[0].d_count = c->counts;
+  c->tree[1].d_count = c->counts + 1;
   *out = c;
   return QBC_OK;
 }
@@ -95,6 +100,10 @@ extern "C" int qbc_destroy(qbc_ctx* c) {
   cudaFree(c->wcount);
   cudaFree(c->wstats);
   cudaFree(c->pixlog);
+  qbc::build_release(&c->build);
+  cudaFree(c->build_input);
+  cudaFree(c->derr);
+  cudaFree(c->counts);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
   return QBC_OK;
@@ -180,16 +189,47 @@ extern "C" int qbc_get_option(qbc_ctx* c, int option, int* value) {
   return fail(QBC_E_ARG, "qbc_get_option: unknown option %d", option);
 }
 
-extern "C" int qbc_synchronize(qbc_ctx* c) {
-  if (!c) return fail(QBC_E_ARG, "qbc_synchronize: null context");
+int check_device_errors(qbc_ctx* c) {
+  unsigned h = 0;
+  QBC_CUDA(cudaMemcpyAsync(&h, c->derr, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
   QBC_CUDA(cudaStreamSynchronize(c->stream));
+  if (!h) return QBC_OK;
+  QBC_CUDA(cudaMemsetAsync(c->derr, 0, sizeof(unsigned), c->stream));
+  QBC_CUDA(cudaStreamSynchronize(c->stream));
+  if (h & qbc::kErrSkinBone) return fail(QBC_E_ARG, "qbc_skin_rigid: a bone index was outside the bone set (point skinned with bone 0)");
+  if (h & qbc::kErrBuildPoint)
+    return fail(QBC_E_ARG, "tree build: a point was negative, too large or not finite (left out of the tree)");
+  return fail(QBC_E_ARG, "tree build: an octet was outside 0..7 (its path left out of the tree)");
+}
+
+int tree_count(qbc_ctx* c, int tree, int64_t* n) {
+  DevTreeBuf& tb = c->tree[tree];
+  if (tb.count_on_device) {
+    int32_t h = 0;
+    QBC_CUDA(cudaMemcpyAsync(&h, tb.d_count, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    QBC_CUDA(cudaStreamSynchronize(c->stream));
+    *n = h;
+  } else {
+    *n = tb.n;
+  }
   return QBC_OK;
 }
 
+extern "C" int qbc_synchronize(qbc_ctx* c) {
+  qbc::clear_error();
+  if (!c) return fail(QBC_E_ARG, "qbc_synchronize: null context");
+  QBC_CUDA(cudaSetDevice(c->device));
+  QBC_CUDA(cudaStreamSynchronize(c->stream));
+  return check_device_errors(c);
+}
+
 extern "C" int qbc_tree_nodes(qbc_ctx* c, int tree, int64_t* n) {
+  qbc::clear_error();
   if (!c || !n || tree < 0 || tree > 1) return fail(QBC_E_ARG, "qbc_tree_nodes: bad argument");
-  *n = c->tree[tree].n;
-  return QBC_OK;
+  QBC_CUDA(cudaSetDevice(c->device));
+  int rc = tree_count(c, tree, n);
+  if (rc) return rc;
+  return check_device_errors(c);
 }
 
 extern "C" int qbc_model_points(qbc_ctx* c, int model, int64_t* n) {
@@ -260,6 +300,7 @@ int upload_impl(qbc_ctx* c, const void* data, int type, size_t size, size_t item
     }
     hi = std::min(hi, n_total);
     t.n = n_total;
+    t.count_on_device = false;
     t.box_valid = false;  // leaf boxes rebuilt before the next render
     const int64_t chunk = (int64_t)(kStageMax / node_bytes);
     if (hi > lo && !device_src) {
@@ -314,7 +355,9 @@ int upload_impl(qbc_ctx* c, const void* data, int type, size_t size, size_t item
       ++c->launches;
     }
   }
-  QBC_CUDA(cudaStreamSynchronize(c->stream));
+  // a host array may be reused once the call returns; a device source is
+  // read in stream order
+  if (!device_src) QBC_CUDA(cudaStreamSynchronize(c->stream));
   return QBC_OK;
 }
 }  // namespace
@@ -332,14 +375,43 @@ struct BoneSet {
 __global__ void skin_rigid_kernel(const float* __restrict__ rp, const float* __restrict__ rn,
                                   const int32_t* __restrict__ bone, int64_t n, int n_bones,
                                   const __grid_constant__ BoneSet bones, float* __restrict__ op,
-                                  float* __restrict__ on, int* __restrict__ bad) {
+                                  float* __restrict__ on, unsigned* __restrict__ bad) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     int b = bone[i];
     if (b < 0 || b >= n_bones) {
-      atomicExch(bad, 1);
+      atomicOr(bad, qbc::kErrSkinBone);
       b = 0;
     }
     const float* m = bones.m[b];
+    const float x = rp[3 * i], y = rp[3 * i + 1], z = rp[3 * i + 2];
+    op[3 * i] = m[0] * x + m[1] * y + m[2] * z + m[9];
+    op[3 * i + 1] = m[3] * x + m[4] * y + m[5] * z + m[10];
+    op[3 * i + 2] = m[6] * x + m[7] * y + m[8] * z + m[11];
+    if (rn && on) {
+      const float a = rn[3 * i], bb = rn[3 * i + 1], cc = rn[3 * i + 2];
+      on[3 * i] = m[0] * a + m[1] * bb + m[2] * cc;
+      on[3 * i + 1] = m[3] * a + m[4] * bb + m[5] * cc;
+      on[3 * i + 2] = m[6] * a + m[7] * bb + m[8] * cc;
+    }
+  }
+}
+
+// The same with the bone set read from device memory when the kernel runs
+// (a captured frame then sees the bones written before each replay).
+__global__ void skin_rigid_dev_kernel(const float* __restrict__ rp, const float* __restrict__ rn,
+                                      const int32_t* __restrict__ bone, int64_t n, int n_bones,
+                                      const float* __restrict__ bones, float* __restrict__ op,
+                                      float* __restrict__ on, unsigned* __restrict__ bad) {
+  __shared__ float m_all[QBC_MAX_BONES * 12];
+  for (int k = threadIdx.x; k < n_bones * 12; k += blockDim.x) m_all[k] = bones[k];
+  __syncthreads();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int b = bone[i];
+    if (b < 0 || b >= n_bones) {
+      atomicOr(bad, qbc::kErrSkinBone);
+      b = 0;
+    }
+    const float* m = m_all + 12 * b;
     const float x = rp[3 * i], y = rp[3 * i + 1], z = rp[3 * i + 2];
     op[3 * i] = m[0] * x + m[1] * y + m[2] * z + m[9];
     op[3 * i + 1] = m[3] * x + m[4] * y + m[5] * z + m[10];
@@ -369,18 +441,10 @@ extern "C" int qbc_skin_rigid(qbc_ctx* c, const float* rest_pnts, const float* r
   BoneSet bs;
   std::memset(&bs, 0, sizeof(bs));
   std::memcpy(bs.m, bones, sizeof(float) * 12 * (size_t)n_bones);
-  int rc = ensure_stage(c, 256);
-  if (rc) return rc;
-  int* bad = (int*)c->stage;
-  QBC_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), c->stream));
   skin_rigid_kernel<<<launch_grid(c, n), 256, 0, c->stream>>>(rest_pnts, rest_nrms, bone, n, n_bones, bs, out_pnts,
-                                                              out_nrms, bad);
+                                                              out_nrms, c->derr);
   QBC_CUDA(cudaGetLastError());
   ++c->launches;
-  int hbad = 0;
-  QBC_CUDA(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  QBC_CUDA(cudaStreamSynchronize(c->stream));
-  if (hbad) return fail(QBC_E_ARG, "qbc_skin_rigid: a bone index is outside 0..%d", n_bones - 1);
   return QBC_OK;
 }
 
@@ -390,21 +454,36 @@ extern "C" int qbc_skin_rigid(qbc_ctx* c, const float* rest_pnts, const float* r
 
 namespace {
 
-int grow_tree_target(qbc::BuildTarget* t, int64_t nodes) {
-  DevTreeBuf& tb = *static_cast<DevTreeBuf*>(t->user);
-  if (nodes > tb.cap) {
-    int64_t cap = nodes + nodes / 8;
-    int rc = grow(&tb.child, &tb.cap, cap, 32, "octree child blocks");
-    if (rc) return rc;
-    int64_t mcap = 0;
-    rc = grow(&tb.model, &mcap, cap, 4, "octree model indices");
+// Host build input is checked here (so a bad point fails the call at once)
+// and copied to the device.
+int stage_build_input(qbc_ctx* c, const float* pnts, const int32_t* octets, int64_t n, int levels,
+                      const void** dev) {
+  if (pnts) {
+    for (int64_t i = 0; i < 3 * n; ++i)
+      if (!(pnts[i] >= 0.0f && pnts[i] < 1.0e30f))
+        return fail(QBC_E_ARG, "tree build: point %lld is negative, too large or not finite", (long long)(i / 3));
+  } else {
+    for (int64_t i = 0; i < n * levels; ++i)
+      if (octets[i] < 0 || octets[i] > 7)
+        return fail(QBC_E_ARG, "tree build: octet %d of path %lld is outside 0..7", octets[i], (long long)(i / levels));
+  }
+  const size_t bytes = pnts ? (size_t)n * 12 : (size_t)n * levels * 4;
+  if (c->build_input_cap < (int64_t)bytes) {
+    int rc = grow(reinterpret_cast<char**>(&c->build_input), &c->build_input_cap, (int64_t)bytes, 1, "tree build input");
     if (rc) return rc;
   }
-  t->child = reinterpret_cast<int32_t*>(tb.child);
-  t->model = tb.model;
+  QBC_CUDA(cudaMemcpyAsync(c->build_input, pnts ? (const void*)pnts : (const void*)octets, bytes,
+                           cudaMemcpyHostToDevice, c->stream));
+  *dev = c->build_input;
   return QBC_OK;
 }
 
+// A GPU build into tree `tree` (qbc_build_tree, qbc_build_tree_paths,
+// qbc_load_flat). Buffers are sized for the build's node bound, so a build of
+// the same size as the last one allocates nothing, and nothing is read back:
+// the exact node count stays on the device. A static-tree build frees the
+// build scratch afterwards (a one-time build); a dynamic-tree build keeps it
+// for the next frame.
 int build_into(qbc_ctx* c, int tree, const float* pnts, const int32_t* octets, int64_t n, float basesize, int levels,
                int64_t first_index, int on_device) {
   if (!c || tree < 0 || tree > 1) return fail(QBC_E_ARG, "tree build: bad context or tree id");
@@ -412,30 +491,46 @@ int build_into(qbc_ctx* c, int tree, const float* pnts, const int32_t* octets, i
   if (pnts && !(basesize > 0.0f)) return fail(QBC_E_ARG, "tree build: basesize must be positive");
   if (levels < 0 || levels > 21) return fail(QBC_E_ARG, "tree build: levels %d outside 0..21", levels);
   QBC_CUDA(cudaSetDevice(c->device));
-  const float* dp = pnts;
-  const int32_t* doc = octets;
-  void* tmp = nullptr;
+  const void* dev = pnts ? (const void*)pnts : (const void*)octets;
   if (!on_device && n > 0) {
-    size_t bytes = pnts ? (size_t)n * 12 : (size_t)n * levels * 4;
-    cudaError_t e = cudaMalloc(&tmp, bytes);
-    if (e != cudaSuccess) return fail(QBC_E_NOMEM, "tree build input of %zu bytes: %s", bytes, cudaGetErrorString(e));
-    e = cudaMemcpyAsync(tmp, pnts ? (const void*)pnts : (const void*)octets, bytes, cudaMemcpyHostToDevice, c->stream);
-    if (e != cudaSuccess) {
-      cudaFree(tmp);
-      return cuda_fail(e, "tree build input copy");
-    }
-    if (pnts)
-      dp = static_cast<const float*>(tmp);
-    else
-      doc = static_cast<const int32_t*>(tmp);
+    int rc = stage_build_input(c, pnts, octets, n, levels, &dev);
+    if (rc) return rc;
   }
-  qbc::BuildTarget t{nullptr, nullptr, 0, 0, &c->tree[tree], grow_tree_target};
-  int rc = qbc::build_nodes(pnts ? dp : nullptr, pnts ? nullptr : doc, n, basesize, levels, first_index, c->stream, &t);
-  if (tmp) cudaFree(tmp);
-  c->launches += t.launches;
+  int rc = qbc::build_reserve(&c->build, n, levels);
   if (rc) return rc;
-  c->tree[tree].n = t.n_nodes;
-  c->tree[tree].box_valid = false;
+  DevTreeBuf& tb = c->tree[tree];
+  const int64_t bound = qbc::build_node_bound(n, levels);
+  if (tb.cap < bound || !tb.child) {
+    int64_t cap = 0;
+    rc = grow(&tb.child, &cap, bound, 32, "octree child blocks");
+    if (!rc) rc = grow(&tb.model, &tb.cap, bound, 4, "octree model indices");
+    if (rc) return rc;
+  }
+  if (tb.cbox_cap < bound || !tb.cbox) {
+    rc = grow(&tb.cbox, &tb.cbox_cap, bound, 64, "octree leaf boxes");
+    if (rc) return rc;
+  }
+  rc = qbc::build_tree_async(pnts ? static_cast<const float*>(dev) : nullptr,
+                             pnts ? nullptr : static_cast<const int32_t*>(dev), n, basesize, levels, first_index,
+                             &c->build, reinterpret_cast<int32_t*>(tb.child), tb.model, tb.cbox, tb.d_count, c->derr,
+                             c->stream, c->sm_count * 8, &c->launches);
+  if (rc) return rc;
+  tb.n = bound;
+  tb.count_on_device = true;
+  tb.box_depth = levels <= QBC_MAX_LEVEL ? levels : -1;
+  tb.box_valid = true;
+  if (tree == 0) {
+    // a one-time build: the exact count bounds the kernels' index checks
+    int64_t exact = 0;
+    rc = tree_count(c, 0, &exact);
+    if (rc) return rc;
+    tb.n = exact;
+    tb.count_on_device = false;
+    qbc::build_release(&c->build);
+    cudaFree(c->build_input);
+    c->build_input = nullptr;
+    c->build_input_cap = 0;
+  }
   return QBC_OK;
 }
 
@@ -449,6 +544,40 @@ __global__ void unpack_nodes_kernel(const int4* __restrict__ child, const int32_
 }
 
 }  // namespace
+
+int dynamic_update(qbc_ctx* c, const qbc_dynamic_update* u) {
+  if (!c || !u) return fail(QBC_E_ARG, "qbc_dynamic_update: null argument");
+  if (u->n < 0 || (u->n > 0 && (!u->rest_pnts || !u->bone || !u->bones || !u->pnts)))
+    return fail(QBC_E_ARG, "qbc_dynamic_update: null array");
+  if (u->n_bones < 1 || u->n_bones > QBC_MAX_BONES)
+    return fail(QBC_E_ARG, "qbc_dynamic_update: %d bones outside 1..%d", u->n_bones, QBC_MAX_BONES);
+  if ((u->rest_nrms == nullptr) != (u->nrms == nullptr))
+    return fail(QBC_E_ARG, "qbc_dynamic_update: give both normal arrays or neither");
+  if (u->n > INT32_MAX) return fail(QBC_E_ARG, "qbc_dynamic_update: %lld points exceed int32 indices", (long long)u->n);
+  QBC_CUDA(cudaSetDevice(c->device));
+  if (u->n > 0) {
+    skin_rigid_dev_kernel<<<launch_grid(c, u->n), 256, 0, c->stream>>>(u->rest_pnts, u->rest_nrms, u->bone, u->n,
+                                                                         u->n_bones, u->bones, u->pnts, u->nrms,
+                                                                         c->derr);
+    QBC_CUDA(cudaGetLastError());
+    ++c->launches;
+  }
+  int64_t n = u->n;
+  const float* pts = u->n > 0 ? u->pnts : reinterpret_cast<const float*>(&n);
+  int rc = build_into(c, 1, pts, nullptr, u->n, u->basesize, u->levels, 0, 1);
+  if (rc) return rc;
+  if (u->nrms && u->n > 0) {
+    const size_t bytes = (size_t)u->n * 12;
+    rc = upload_impl(c, u->nrms, QBC_GL_FLOAT, bytes, 12, 0, bytes, QBC_DYNAMIC_NORMAL, true);
+  }
+  return rc;
+}
+
+extern "C" int qbc_dynamic_update_run(qbc_ctx* c, const qbc_dynamic_update* u) {
+  qbc::clear_error();
+  return dynamic_update(c, u);
+}
+
 
 extern "C" int qbc_build_tree(qbc_ctx* c, int tree, const float* pnts, int64_t n, float basesize, int levels,
                               int64_t first_index, int on_device) {
@@ -500,7 +629,10 @@ extern "C" int qbc_load_flat(qbc_ctx* c, int tree, const char* pnt_path, const c
   rc = build_into(c, tree, src, nullptr, n, basesize, levels, 0, 0);
   if (rc) return rc;
   if (points) *points = n;
-  if (nodes) *nodes = c->tree[tree].n;
+  if (nodes) {
+    int rc2 = tree_count(c, tree, nodes);
+    if (rc2) return rc2;
+  }
   if (range_ints) *range_ints = nr;
   return QBC_OK;
 }
@@ -560,7 +692,11 @@ extern "C" int qbc_tree_remove_points(qbc_ctx* c, int tree, const float* pts, in
 extern "C" int qbc_download_tree(qbc_ctx* c, int tree, int32_t* nodes, int64_t cap, int64_t* n_nodes) {
   qbc::clear_error();
   if (!c || tree < 0 || tree > 1 || !n_nodes) return fail(QBC_E_ARG, "qbc_download_tree: bad argument");
-  const int64_t n = c->tree[tree].n;
+  QBC_CUDA(cudaSetDevice(c->device));
+  int64_t n = 0;
+  int rc0 = tree_count(c, tree, &n);
+  if (!rc0) rc0 = check_device_errors(c);
+  if (rc0) return rc0;
   *n_nodes = n;
   if (!nodes || n == 0) return QBC_OK;
   if (cap < n) return fail(QBC_E_ARG, "qbc_download_tree: capacity %lld below %lld nodes", (long long)cap, (long long)n);
@@ -831,8 +967,11 @@ int check_render_opts(const qbc_render_opts* opts, int n) {
     return fail(QBC_E_ARG, "qbc_render_views_ex: proposals need two_pass");
   if (opts && (opts->proposal_level < 0 || opts->proposal_level > QBC_MAX_LEVEL))
     return fail(QBC_E_ARG, "qbc_render_views_ex: proposal_level %d outside 0..%d", opts->proposal_level, QBC_MAX_LEVEL);
-  if (opts && opts->two_pass && n > qbc::kMaxViewsPerLaunch)
-    return fail(QBC_E_ARG, "qbc_render_views_ex: two-pass renders take at most %d views per call", qbc::kMaxViewsPerLaunch);
+  // the render log indexes pixels within one launch of kMaxViewsPerLaunch
+  // views; other two-pass renders run batch after batch
+  if (opts && opts->two_pass && (opts->log || opts->proposals == QBC_PROPOSE_LOGGED) && n > qbc::kMaxViewsPerLaunch)
+    return fail(QBC_E_ARG, "qbc_render_views_ex: logged two-pass renders take at most %d views per call",
+                qbc::kMaxViewsPerLaunch);
   return QBC_OK;
 }
 

@@ -201,6 +201,25 @@ class OctreeGLC:
         check(self._lib.qbc_graph_capture(self.handle, varr, oarr, n, C.byref(opts), C.byref(h)))
         return FrameGraph(self, h, n)
 
+    def dynamic_update(self, update: "_lib.DynamicUpdate") -> None:
+        """qbc_dynamic_update_run: skin, rebuild the dynamic tree, take the
+        normals, all queued on the context's stream."""
+        check(self._lib.qbc_dynamic_update_run(self.handle, C.byref(update)))
+
+    def graph_capture_dynamic(self, update: "_lib.DynamicUpdate", views: Sequence[View],
+                              outputs: Sequence[Outputs], two_pass: bool = False, proposals: int = 0,
+                              proposal_level: int = 0, seed: int = 0) -> "FrameGraph":
+        """qbc_graph_capture_dynamic: the dynamic update and the frame as one
+        CUDA graph; write new bones into update.bones before each launch."""
+        n = len(views)
+        varr = (View * n)(*views)
+        oarr = (Outputs * n)(*outputs)
+        opts = _lib.RenderOpts(int(two_pass), int(proposals), 0, int(proposal_level), int(seed))
+        h = C.c_void_p()
+        check(self._lib.qbc_graph_capture_dynamic(self.handle, C.byref(update), varr, oarr, n, C.byref(opts),
+                                                  C.byref(h)))
+        return FrameGraph(self, h, n)
+
     def render_views_noalloc(self, views: Sequence[View], outputs: Sequence[Outputs]) -> None:
         """qbc_render_views_noalloc: device outputs only, no allocation in
         the call (the work-queue counters live in static device memory)."""
@@ -245,9 +264,10 @@ class OctreeGLC:
         check(self._lib.qbc_set_stream(self.handle, C.c_void_p(stream_ptr or 0)))
 
     def build_tree(self, dynamic: bool, points, basesize: float = 1800.0, levels: int = 12,
-                   first_index: int = 0) -> int:
+                   first_index: int = 0, count: bool = True) -> Optional[int]:
         """GPU build of the static or dynamic tree from points (numpy host
-        array, or a device pointer with `points=(ptr, n)`); returns the node count."""
+        array, or a device pointer with `points=(ptr, n)`); returns the node
+        count (count=False: returns None and does not wait for the build)."""
         if isinstance(points, tuple):
             ptr, n, dev = int(points[0]), int(points[1]), 1
         else:
@@ -255,7 +275,7 @@ class OctreeGLC:
             ptr, n, dev = p.ctypes.data, p.shape[0], 0
         check(self._lib.qbc_build_tree(self.handle, 1 if dynamic else 0, C.c_void_p(ptr), n, float(basesize),
                                        int(levels), int(first_index), dev))
-        return self.tree_nodes(1 if dynamic else 0)
+        return self.tree_nodes(1 if dynamic else 0) if count else None
 
     def build_tree_paths(self, dynamic: bool, octets, levels: int = 12, first_index: int = 0) -> int:
         if isinstance(octets, tuple):

@@ -216,6 +216,12 @@ WORKLOADS = {
 _b64_sizes, _b64_poses = batch_views(64, 64)
 WORKLOADS["floor1m_char2m_mixed_x64"] = Workload("floor1m_char2m_mixed_x64", "floor1m", 0, 0, _b64_poses,
                                                  sizes=_b64_sizes, character=2_000_000)
+# the same batch with the occluder-proposal network: trained (untimed) on the
+# plain walk's shadow rays of 256 other ring poses at 960x720, the character
+# in its first pose
+WORKLOADS["floor1m_char2m_mlp_mixed_x64"] = Workload("floor1m_char2m_mlp_mixed_x64", "floor1m", 0, 0, _b64_poses,
+                                                     sizes=_b64_sizes, character=2_000_000,
+                                                     train_poses=batch_views(3001, 256)[1])
 # one 1920x1080 view of the same floor and 2M-point character (camera on the
 # ring, aimed at the character): a small case of the two-tree kernel for
 # profiling

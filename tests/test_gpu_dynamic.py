@@ -38,6 +38,7 @@ def test_character_frames(oracle, floor50k_scene):
             ctx.skin_rigid(rp.data_ptr(), rn.data_ptr(), bone.data_ptr(), n, bones, op.data_ptr(), on.data_ptr())
             ctx.build_tree(True, (op.data_ptr(), n), S, LEVELS)
             ctx.upload_device(on.data_ptr(), qb.GL_FLOAT, n * 12, 12, 0, n * 12, qb.OCTREE_GLC_BUFFER_DYNAMIC_NORMAL)
+            ctx.synchronize()
             p_ref, n_ref = scenes.skin_reference(ch, bones)
             np.testing.assert_array_equal(op.cpu().numpy().view(np.uint32), p_ref.view(np.uint32))
             np.testing.assert_array_equal(on.cpu().numpy().view(np.uint32), n_ref.view(np.uint32))
@@ -62,7 +63,12 @@ def test_skin_rejects_bad_bone(floor50k_scene):
         b = torch.tensor([0, 1, 5, 0], dtype=torch.int32, device="cuda")
         o = torch.empty_like(p)
         bones = np.zeros((2, 12), np.float32)
-        with pytest.raises(qb.QbcError):
-            ctx.skin_rigid(p.data_ptr(), 0, b.data_ptr(), 4, bones, o.data_ptr(), 0)
+        # the kernel cannot stop: it skins with bone 0 and the next call
+        # that synchronizes reports the fault (once)
+        ctx.skin_rigid(p.data_ptr(), 0, b.data_ptr(), 4, bones, o.data_ptr(), 0)
+        with pytest.raises(qb.QbcError) as e:
+            ctx.synchronize()
+        assert "bone" in str(e.value)
+        ctx.synchronize()
     finally:
         ctx.close()
