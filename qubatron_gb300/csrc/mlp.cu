@@ -2,13 +2,14 @@
 // BF16 weights and activations on the tensor cores with FP32 accumulation,
 // trained on the GPU with hand-written forward, backward and Adam kernels.
 //
-// Every matrix product goes through one kernel, gemm_kernel: a 64x64 output
-// tile per block of 4 warps, operands staged in shared memory in 32-deep K
-// slices, fragments loaded with ldmatrix and multiplied with
-// mma.sync.m16n8k16 (bf16 x bf16 -> f32). The epilogue adds the bias, applies
-// GELU, stores the pre-activation (for backward) and the bf16 activation, or
-// accumulates into an fp32 result with atomics (weight gradients, where the
-// reduction runs over the batch and is split across blocks).
+// Every matrix product goes through one kernel, gemm_kernel, on the tcgen05
+// tensor cores: a 128 x 64 output tile per block of 4 warps in a tensor-memory
+// accumulator, operands staged in shared memory in 32-deep K slices (two
+// stages, transposed as the product needs), bf16 x bf16 -> f32. The epilogue
+// reads the accumulator with tcgen05.ld, adds the bias, applies GELU, stores
+// the pre-activation (for backward) and the bf16 activation, or accumulates
+// into an fp32 result with atomics (weight gradients, where the reduction
+// runs over the batch and is split across blocks).
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -36,9 +37,30 @@ namespace {
 
 using bf16 = __nv_bfloat16;
 
-constexpr int kTile = 64;
-constexpr int kKs = 32;          // K slice per shared-memory stage
-constexpr int kLd = kKs + 8;     // padded row: 80 B, conflict-free ldmatrix
+// GEMM tiles on the tcgen05 tensor cores: a block computes a 128 (M) x 64 (N)
+// tile of C into a 64-column fp32 accumulator in tensor memory, with K in
+// slices of 32 staged by the block's threads into one of two shared-memory
+// stages (K-major core-matrix layout, umma.cuh; op(A) and op(B) transposed
+// while staging) while the previous slice's MMAs run.
+constexpr int kTileM = 128;
+constexpr int kTileN = 64;
+constexpr int kKs = 32;
+constexpr int kGemmThreads = 128;
+constexpr uint32_t kGemmTmemCols = 64;
+// dynamic shared memory per block: two stages of A (8 KB) and B (4 KB), the
+// barriers, and headroom that keeps at most 7 blocks on an SM (7 x 64 of its
+// 512 tensor-memory columns)
+constexpr int kGemmSmemBytes = 32 * 1024;
+
+struct GemmSmem {
+  bf16 a[2][kTileM * kKs];
+  bf16 b[2][kTileN * kKs];
+  uint64_t bar[2];
+  uint64_t done;
+  uint32_t tmem;
+  uint32_t fault;
+};
+static_assert(sizeof(GemmSmem) + 1024 <= kGemmSmemBytes, "gemm shared memory");
 
 struct Epi {
   float* C;         // fp32 output (or atomic accumulator)
@@ -50,6 +72,7 @@ struct Epi {
   const float* bias;
   int gelu;
   int atomic;
+  unsigned* err;    // kErrMmaTimeout when a tensor-core wait gave up
 };
 
 __device__ __forceinline__ float gelu_grad(float x) {
@@ -62,89 +85,106 @@ __device__ __forceinline__ float gelu_grad(float x) {
 // K x M row-major (TA true); B is K x N row-major (TB false) or N x K
 // row-major (TB true). Block z handles K rows [z * kchunk, (z + 1) * kchunk).
 template <bool TA, bool TB>
-__global__ void __launch_bounds__(128) gemm_kernel(const bf16* __restrict__ A, int lda, const bf16* __restrict__ B,
-                                                   int ldb, int M, int N, int K, int kchunk, Epi epi) {
-  __shared__ __align__(16) bf16 As[kTile][kLd];
-  __shared__ __align__(16) bf16 Bs[kTile][kLd];
+__global__ void __launch_bounds__(kGemmThreads) gemm_kernel(const bf16* __restrict__ A, int lda,
+                                                            const bf16* __restrict__ B, int ldb, int M, int N, int K,
+                                                            int kchunk, Epi epi) {
+  extern __shared__ unsigned char gemm_smem_raw[];
+  GemmSmem& S = *reinterpret_cast<GemmSmem*>((reinterpret_cast<uintptr_t>(gemm_smem_raw) + 1023) &
+                                             ~static_cast<uintptr_t>(1023));
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int m0 = blockIdx.y * kTile, n0 = blockIdx.x * kTile;
+  const int m0 = blockIdx.y * kTileM, n0 = blockIdx.x * kTileN;
   const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
-  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
-  float acc[2][4][4];
-#pragma unroll
-  for (int i = 0; i < 2; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-#pragma unroll
-      for (int r = 0; r < 4; ++r) acc[i][j][r] = 0.0f;
-  const bf16 zero = __float2bfloat16(0.0f);
-
-  for (int k0 = kb; k0 < ke; k0 += kKs) {
-    // stage op(A)[m0.., k0..] as As[m][k] and op(B)[k0.., n0..] as Bs[n][k],
-    // consecutive threads along each operand's contiguous dimension
-    for (int e = tid; e < kTile * kKs; e += 128) {
-      const int r = TA ? e % kTile : e / kKs, c = TA ? e / kTile : e % kKs;  // r: m, c: k
-      const int m = m0 + r, k = k0 + c;
-      bf16 a = zero;
-      if (m < M && k < ke) a = TA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k];
-      As[r][c] = a;
-    }
-    for (int e = tid; e < kTile * kKs; e += 128) {
-      const int r = TB ? e / kKs : e % kTile, c = TB ? e % kKs : e / kTile;  // r: n, c: k
-      const int n = n0 + r, k = k0 + c;
-      bf16 b = zero;
-      if (n < N && k < ke) b = TB ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n];
-      Bs[r][c] = b;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < kKs; kk += 16) {
-      uint32_t af[2][4];
-#pragma unroll
-      for (int mi = 0; mi < 2; ++mi) {
-        const int row = wm + mi * 16 + (lane & 15);
-        const int col = kk + (lane >> 4) * 8;
-        ldsm_x4(smem_u32(&As[row][col]), af[mi][0], af[mi][1], af[mi][2], af[mi][3]);
-      }
-#pragma unroll
-      for (int nj = 0; nj < 4; nj += 2) {
-        const int row = wn + nj * 8 + (lane & 7) + ((lane >> 4) << 3);
-        const int col = kk + ((lane >> 3) & 1) * 8;
-        uint32_t b0, b1, b2, b3;
-        ldsm_x4(smem_u32(&Bs[row][col]), b0, b1, b2, b3);
-#pragma unroll
-        for (int mi = 0; mi < 2; ++mi) {
-          mma_bf16(acc[mi][nj], af[mi], b0, b1);
-          mma_bf16(acc[mi][nj + 1], af[mi], b2, b3);
-        }
-      }
-    }
-    __syncthreads();
+  if (tid == 0) {
+    S.fault = 0u;
+    umma::mbar_init(&S.bar[0], 1);
+    umma::mbar_init(&S.bar[1], 1);
+    umma::mbar_init(&S.done, 1);
   }
-
-  const int g = lane >> 2, t = lane & 3;
+  if (warp == 0) {
+    umma::tmem_alloc(&S.tmem, kGemmTmemCols);
+    umma::tmem_relinquish();
+  }
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  const uint32_t tmem = S.tmem;
+  const uint32_t idesc = umma::idesc_bf16(kTileM, kTileN);
+  const bf16 zero = __float2bfloat16(0.0f);
+  uint32_t ph[2] = {0u, 0u};
+  int it = 0;
+  for (int k0 = kb; k0 < ke; k0 += kKs, ++it) {
+    const int st = it & 1;
+    if (it >= 2) {  // the MMAs of slice it - 2 have read this stage
+      if (!umma::mbar_wait(&S.bar[st], ph[st], kUmmaWaitLimit)) atomicOr(&S.fault, 1u);
+      ph[st] ^= 1u;
+    }
+    // stage op(A)[m0.., k0..] and op(B)[k0.., n0..] (consecutive threads
+    // along each operand's contiguous dimension)
+    char* as = reinterpret_cast<char*>(S.a[st]);
+    char* bs = reinterpret_cast<char*>(S.b[st]);
+    for (int e = tid; e < kTileM * kKs; e += kGemmThreads) {
+      const int r = TA ? e % kTileM : e / kKs, c = TA ? e / kTileM : e % kKs;  // r: m, c: k
+      const int m = m0 + r, k = k0 + c;
+      bf16 v = zero;
+      if (m < M && k < ke) v = TA ? A[(size_t)k * lda + m] : A[(size_t)m * lda + k];
+      *reinterpret_cast<bf16*>(as + umma::core_offset(r, c, kKs)) = v;
+    }
+    for (int e = tid; e < kTileN * kKs; e += kGemmThreads) {
+      const int r = TB ? e / kKs : e % kTileN, c = TB ? e % kKs : e / kTileN;  // r: n, c: k
+      const int n = n0 + r, k = k0 + c;
+      bf16 v = zero;
+      if (n < N && k < ke) v = TB ? B[(size_t)n * ldb + k] : B[(size_t)k * ldb + n];
+      *reinterpret_cast<bf16*>(bs + umma::core_offset(r, c, kKs)) = v;
+    }
+    umma::fence_smem_to_async();
+    umma::fence_before_sync();
+    __syncthreads();
+    if (S.fault) break;
+    if (tid == 0) {
+      umma::fence_after_sync();
+      const uint32_t sa = umma::smem_addr(as), sb = umma::smem_addr(bs);
 #pragma unroll
-  for (int mi = 0; mi < 2; ++mi) {
+      for (int kk = 0; kk < kKs; kk += 16)
+        umma::mma_bf16(tmem, umma::slice_desc(sa, kk, kKs), umma::slice_desc(sb, kk, kKs), idesc,
+                       it > 0 || kk > 0);
+      umma::commit(&S.bar[st]);
+    }
+  }
+  // every MMA of this block done
+  if (tid == 0) umma::commit(&S.done);
+  if (!umma::mbar_wait(&S.done, 0, kUmmaWaitLimit)) atomicOr(&S.fault, 1u);
+  umma::fence_after_sync();
+  __syncthreads();
+  if (S.fault) {
+    if (tid == 0 && epi.err) atomicOr(epi.err, kErrMmaTimeout);
+  } else {
+    float v[2][32];
+    umma::tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16), v[0]);
+    umma::tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + 32, v[1]);
+    umma::tmem_ld_wait();
+    const int m = m0 + 32 * warp + lane;
+    if (m < M) {
 #pragma unroll
-    for (int nj = 0; nj < 4; ++nj) {
-#pragma unroll
-      for (int r = 0; r < 4; ++r) {
-        const int m = m0 + wm + mi * 16 + g + (r >> 1) * 8;
-        const int n = n0 + wn + nj * 8 + 2 * t + (r & 1);
-        if (m >= M || n >= N) continue;
-        float v = acc[mi][nj][r];
+      for (int j = 0; j < kTileN; ++j) {
+        const int n = n0 + j;
+        if (n >= N) break;
+        float x = it > 0 ? v[j >> 5][j & 31] : 0.0f;
         if (epi.atomic) {
-          atomicAdd(&epi.C[(size_t)m * epi.ldc + n], v);
+          if (it > 0) atomicAdd(&epi.C[(size_t)m * epi.ldc + n], x);
           continue;
         }
-        if (epi.bias) v += epi.bias[n];
-        if (epi.Z) epi.Z[(size_t)m * epi.ldz + n] = v;
-        if (epi.gelu) v = gelu_f(v);
-        if (epi.C) epi.C[(size_t)m * epi.ldc + n] = v;
-        if (epi.Cb) epi.Cb[(size_t)m * epi.ldcb + n] = __float2bfloat16(v);
+        if (epi.bias) x += epi.bias[n];
+        if (epi.Z) epi.Z[(size_t)m * epi.ldz + n] = x;
+        if (epi.gelu) x = gelu_f(x);
+        if (epi.C) epi.C[(size_t)m * epi.ldc + n] = x;
+        if (epi.Cb) epi.Cb[(size_t)m * epi.ldcb + n] = __float2bfloat16(x);
       }
     }
   }
+  umma::fence_before_sync();
+  __syncthreads();
+  umma::fence_after_sync();
+  if (warp == 0) umma::tmem_dealloc(tmem, kGemmTmemCols);
 }
 
 template <bool TA, bool TB>
@@ -153,10 +193,18 @@ int gemm(const bf16* A, int lda, const bf16* B, int ldb, int64_t M, int N, int64
   if (M <= 0 || N <= 0 || K <= 0) return QBC_OK;
   if (kchunk <= 0) kchunk = K;
   kchunk = (kchunk + kKs - 1) / kKs * kKs;
-  dim3 grid((unsigned)((N + kTile - 1) / kTile), (unsigned)((M + kTile - 1) / kTile),
+  dim3 grid((unsigned)((N + kTileN - 1) / kTileN), (unsigned)((M + kTileM - 1) / kTileM),
             (unsigned)((K + kchunk - 1) / kchunk));
   if (grid.y > 65535u) return fail(QBC_E_ARG, "mlp gemm: %lld rows exceed one launch", (long long)M);
-  gemm_kernel<TA, TB><<<grid, 128, 0, s>>>(A, lda, B, ldb, (int)M, N, (int)K, (int)kchunk, epi);
+  static bool attr[4] = {false, false, false, false};
+  const int v = (TA ? 1 : 0) + (TB ? 2 : 0);
+  if (!attr[v]) {
+    cudaError_t e = cudaFuncSetAttribute(gemm_kernel<TA, TB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kGemmSmemBytes);
+    if (e != cudaSuccess) return fail(QBC_E_CUDA, "mlp gemm attribute: %s", cudaGetErrorString(e));
+    attr[v] = true;
+  }
+  gemm_kernel<TA, TB><<<grid, kGemmThreads, kGemmSmemBytes, s>>>(A, lda, B, ldb, (int)M, N, (int)K, (int)kchunk, epi);
   ++g_launches;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(QBC_E_CUDA, "mlp gemm launch: %s", cudaGetErrorString(e));
@@ -410,13 +458,13 @@ int Net::forward(const bf16* X, int64_t rows, float* out, cudaStream_t s, bool k
     const bf16* in = X + r0 * kIn;
     int ld = kIn;
     for (int l = 0; l < 3; ++l) {
-      Epi e{nullptr, 0, b.A[l], kHidden, keep ? b.Z[l] : nullptr, kHidden, bsv[l], 1, 0};
+      Epi e{nullptr, 0, b.A[l], kHidden, keep ? b.Z[l] : nullptr, kHidden, bsv[l], 1, 0, err};
       rc = gemm<false, true>(in, ld, W[l], l == 0 ? kIn : kHidden, n, kHidden, l == 0 ? kIn : kHidden, e, s);
       if (rc) return rc;
       in = b.A[l];
       ld = kHidden;
     }
-    Epi e{out + r0 * kOutPad, kOutPad, nullptr, 0, nullptr, 0, bsv[3], 0, 0};
+    Epi e{out + r0 * kOutPad, kOutPad, nullptr, 0, nullptr, 0, bsv[3], 0, 0, err};
     rc = gemm<false, true>(in, kHidden, W[3], kHidden, n, kOutPad, kHidden, e, s);
     if (rc) return rc;
   }
@@ -440,12 +488,12 @@ int Net::gradient(const bf16* X, const float* tlab, const int8_t* kind, int64_t 
   const int64_t kchunk = 4096;
   // layer 4: dW4 = dO^T A3, db4 = sum dO, dA3 = dO W4
   {
-    Epi e{grad + param_offset(3, false), kHidden, nullptr, 0, nullptr, 0, nullptr, 0, 1};
+    Epi e{grad + param_offset(3, false), kHidden, nullptr, 0, nullptr, 0, nullptr, 0, 1, err};
     rc = gemm<true, false>(b.dO, kOutPad, b.A[2], kHidden, kOutPad, kHidden, rows, e, s, kchunk);
     if (rc) return rc;
     bias_grad_kernel<<<kOutPad, 256, 0, s>>>(b.dO, rows, kOutPad, grad + param_offset(3, true));
     ++g_launches;
-    Epi d{b.dA, kHidden, nullptr, 0, nullptr, 0, nullptr, 0, 0};
+    Epi d{b.dA, kHidden, nullptr, 0, nullptr, 0, nullptr, 0, 0, err};
     rc = gemm<false, false>(b.dO, kOutPad, W[3], kHidden, rows, kHidden, kOutPad, d, s);
     if (rc) return rc;
   }
@@ -454,13 +502,13 @@ int Net::gradient(const bf16* X, const float* tlab, const int8_t* kind, int64_t 
     ++g_launches;
     const bf16* prev = l > 0 ? b.A[l - 1] : X;
     const int kin = l > 0 ? kHidden : kIn;
-    Epi e{grad + param_offset(l, false), kin, nullptr, 0, nullptr, 0, nullptr, 0, 1};
+    Epi e{grad + param_offset(l, false), kin, nullptr, 0, nullptr, 0, nullptr, 0, 1, err};
     rc = gemm<true, false>(b.dZ, kHidden, prev, kin, kHidden, kin, rows, e, s, kchunk);
     if (rc) return rc;
     bias_grad_kernel<<<kHidden, 256, 0, s>>>(b.dZ, rows, kHidden, grad + param_offset(l, true));
     ++g_launches;
     if (l > 0) {
-      Epi d{b.dA, kHidden, nullptr, 0, nullptr, 0, nullptr, 0, 0};
+      Epi d{b.dA, kHidden, nullptr, 0, nullptr, 0, nullptr, 0, 0, err};
       rc = gemm<false, false>(b.dZ, kHidden, W[l], kin, rows, kin, kHidden, d, s);
       if (rc) return rc;
     }

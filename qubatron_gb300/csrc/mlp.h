@@ -34,6 +34,7 @@ struct Net {
   int64_t work_rows = 0;
   int64_t step_count = 0;
   bool ready = false;
+  unsigned* err = nullptr;       // device error word of the owning context
 
   int init(uint64_t seed, cudaStream_t s);
   int set(const float* host, cudaStream_t s);

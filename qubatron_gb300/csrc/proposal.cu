@@ -158,18 +158,18 @@ bf16 host_bf16(float f) {
   return __ushort_as_bfloat16((unsigned short)(u >> 16));
 }
 
-// One launch of the fused network over `src`'s rows: a persistent grid of
-// resident blocks, each staging the weights once.
+// One launch of the network over `src`'s rows on the tcgen05 tensor cores: a
+// persistent grid of one block per SM, each staging the weights once.
 template <class Src>
 int launch_fused(qbc_ctx* c, const Src& src, int variant) {
-  using qbc::mlp::FusedSmem;
-  auto kern = qbc::mlp::fused_forward_kernel<Src>;
+  auto kern = qbc::mlp::umma_forward_kernel<Src>;
+  const int smem = (int)qbc::mlp::kUmmaSmemBytes;
   if (!c->fused_attr[variant]) {
-    QBC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(FusedSmem)));
+    QBC_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     c->fused_attr[variant] = true;
   }
   int per_sm = 0;
-  QBC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, qbc::mlp::kFusedThreads, sizeof(FusedSmem)));
+  QBC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, qbc::mlp::kUmmaThreads, smem));
   if (per_sm < 1) return fail(QBC_E_STATE, "proposal network: no block fits on an SM");
   qbc::mlp::FusedParams p;
   for (int l = 0; l < 4; ++l) {
@@ -177,7 +177,8 @@ int launch_fused(qbc_ctx* c, const Src& src, int variant) {
     p.b[l] = c->net.master + qbc::mlp::param_offset(l, true);
     if (reinterpret_cast<uintptr_t>(p.w[l]) % 16) return fail(QBC_E_STATE, "proposal network: unaligned weights");
   }
-  kern<<<per_sm * c->sm_count, qbc::mlp::kFusedThreads, sizeof(FusedSmem), c->stream>>>(p, src);
+  // one block per SM: each holds 256 of the SM's 512 tensor-memory columns
+  kern<<<c->sm_count, qbc::mlp::kUmmaThreads, smem, c->stream>>>(p, src, c->derr);
   QBC_CUDA(cudaGetLastError());
   ++c->launches;
   return QBC_OK;

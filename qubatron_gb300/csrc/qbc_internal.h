@@ -25,6 +25,7 @@ enum DeviceError : unsigned {
   kErrBuildPoint = 1u,  // a point to build from was negative, too large or not finite
   kErrBuildOctet = 2u,  // an octet path entry was outside 0..7
   kErrSkinBone = 4u,    // a skinned point named a bone outside the bone set
+  kErrMmaTimeout = 8u,  // a bounded wait for the tensor cores gave up (the kernel stopped early)
 };
 
 // Scratch of the GPU tree build, owned by the context and reused by every

@@ -70,6 +70,7 @@ extern "C" int qbc_create(int device, qbc_ctx** out) {
     return cuda_fail(e, "qbc_create");
   }
   c->stream = c->own;
+  c->net.err = c->derr;
   c->tree[0].d_count = c->counts;
   c->tree[1].d_count = c->counts + 1;
   *out = c;
@@ -196,6 +197,8 @@ int check_device_errors(qbc_ctx* c) {
   if (!h) return QBC_OK;
   QBC_CUDA(cudaMemsetAsync(c->derr, 0, sizeof(unsigned), c->stream));
   QBC_CUDA(cudaStreamSynchronize(c->stream));
+  if (h & qbc::kErrMmaTimeout)
+    return fail(QBC_E_TIMEOUT, "proposal network: a tensor-core wait gave up; the proposals of that render are incomplete");
   if (h & qbc::kErrSkinBone) return fail(QBC_E_ARG, "qbc_skin_rigid: a bone index was outside the bone set (point skinned with bone 0)");
   if (h & qbc::kErrBuildPoint)
     return fail(QBC_E_ARG, "tree build: a point was negative, too large or not finite (left out of the tree)");
