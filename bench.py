@@ -447,17 +447,26 @@ def proposal_comparison(args, device: int, stream, flush) -> dict:
         out["rays_per_frame"] = rays
 
         mlp_kw = dict(two_pass=True, proposals=lib.PROPOSE_MLP, proposal_level=args.proposal_level)
+        # learned: schedule and proposal settings (gate with "off", count,
+        # level) tuned on the frame; learned_fixed: the same schedule with
+        # the default proposal settings (gate 500, 3 proposals, level 8)
         arms = [("plain_fused", {}, 1), ("plain_two_pass", {"two_pass": True}, 1), ("learned", mlp_kw, 1),
-                ("plain_simple", {}, 0)]
+                ("learned_fixed", mlp_kw, 1), ("plain_simple", {}, 0)]
         base = (ctx.get_option(lib.OPT_TILE_WIDTH), ctx.get_option(lib.OPT_BLOCKS_PER_SM),
                 ctx.get_option(lib.OPT_SERVICE_MIN))
+        fixed = {lib.OPT_PROPOSAL_GATE: 500, lib.OPT_PROPOSAL_COUNT: 3, lib.OPT_PROPOSAL_LEVEL: 8}
         res = {}
         for name, kw, persistent in arms:
-            ctx.set_option(lib.OPT_TILE_WIDTH, base[0])
-            ctx.set_option(lib.OPT_BLOCKS_PER_SM, base[1])
-            ctx.set_option(lib.OPT_SERVICE_MIN, base[2])
             ctx.set_option(lib.OPT_PERSISTENT, persistent)
-            tuning = ctx.autotune(views, outs, reps=3, **kw) if args.autotune else None
+            if name == "learned_fixed":
+                for k, v in fixed.items():
+                    ctx.set_option(k, v)
+                tuning = {"schedule": "as learned", "proposal_gate": 500, "proposal_count": 3, "proposal_level": 8}
+            else:
+                ctx.set_option(lib.OPT_TILE_WIDTH, base[0])
+                ctx.set_option(lib.OPT_BLOCKS_PER_SM, base[1])
+                ctx.set_option(lib.OPT_SERVICE_MIN, base[2])
+                tuning = ctx.autotune(views, outs, reps=3, **kw) if args.autotune else None
             g = ctx.graph_capture(views, outs, **kw)
             ms = time_steps(g.launch, stream, flush, args.warmup, args.steps)
             g.close()
@@ -499,22 +508,28 @@ def proposal_comparison(args, device: int, stream, flush) -> dict:
             r["parity_sample"] = {"pixels": n, "rgba8_mismatch": bad8, "flags_mismatch": badf,
                                   "leaf_mismatch": badl}
             del r["frame"]
-        two, mlp = res["plain_two_pass"]["stats"], res["learned"]["stats"]
-        vis_mlp = mlp["shadow_visits"] + mlp["proposal_visits"]
+        two = res["plain_two_pass"]["stats"]
+        for name in ("learned", "learned_fixed"):
+            m = res[name]["stats"]
+            vis = m["shadow_visits"] + m["proposal_visits"]
+            res[name]["proposals"] = {
+                "tried": m["proposals_tried"], "proven": m["proposals_proven"],
+                "hit_rate": m["proposals_proven"] / max(1, m["proposals_tried"]),
+                "shadow_visits": vis, "visits_saved_frac": 1.0 - vis / max(1, two["shadow_visits"])}
         for r in res.values():
             del r["stats"]
         out["arms"] = res
         ms_learned = res["learned"]["ms_per_frame"]
+        tuned_gate = (res["learned"]["tuning"] or {}).get("proposal_gate")
         out.update({
             "speedup_vs_plain_fused": res["plain_fused"]["ms_per_frame"] / ms_learned,
             "speedup_vs_plain_two_pass": res["plain_two_pass"]["ms_per_frame"] / ms_learned,
             "speedup_vs_plain_simple": res["plain_simple"]["ms_per_frame"] / ms_learned,
+            "learned_fixed_speedup_vs_plain_two_pass": res["plain_two_pass"]["ms_per_frame"]
+            / res["learned_fixed"]["ms_per_frame"],
             "persistent_speedup_vs_plain_simple": res["plain_simple"]["ms_per_frame"] / res["plain_fused"]["ms_per_frame"],
-            "shadow_rays": two["shadow_rays"], "proposals_tried": mlp["proposals_tried"],
-            "proposals_proven": mlp["proposals_proven"],
-            "hit_rate": mlp["proposals_proven"] / max(1, mlp["proposals_tried"]),
-            "shadow_visits_plain": two["shadow_visits"], "shadow_visits_learned": vis_mlp,
-            "visits_saved_frac": 1.0 - vis_mlp / max(1, two["shadow_visits"]),
+            "network_switched_off_by_autotuner": tuned_gate == 1000,
+            "shadow_rays": two["shadow_rays"], "shadow_visits_plain": two["shadow_visits"],
             "cpu_oracle": {k: v for k, v in sample.items() if k not in ("seconds", "rays", "parity")},
         })
     finally:
@@ -847,7 +862,8 @@ def main():
     ap.add_argument("--no-graph", dest="graph", action="store_false",
                     help="time eager launches instead of CUDA graph replays of the frame")
     ap.add_argument("--proposal-gate", type=int, default=500, help="occlusion probability (per mille) to try")
-    ap.add_argument("--proposal-level", type=int, default=8, help="octree level of the proposed cells")
+    ap.add_argument("--proposal-level", type=int, default=0,
+                    help="octree level of the proposed cells (0: the context's, swept by the autotuner)")
     ap.add_argument("--proposal-count", type=int, default=3, help="network proposals tried per pixel (1..3)")
     ap.add_argument("--no-proposal-block", action="store_true",
                     help="skip the learned-vs-plain comparison on the proposal workload")

@@ -308,7 +308,8 @@ int qbc_render_views_noalloc(qbc_ctx* ctx, const qbc_view* views, const qbc_outp
  *                   QBC_PROPOSE_RANDOM (seeded, for tests).
  *   log             (two_pass only) record, per queued pixel, the t of the
  *                   plain shadow walk's first leaf and its lit bit.
- *   proposal_level  level of the proposed cells (default 8 when 0).
+ *   proposal_level  level of the proposed cells (0: QBC_OPT_PROPOSAL_LEVEL,
+ *                   default 8).
  *   seed            QBC_PROPOSE_RANDOM seed.
  * A proposal is a point on the shadow ray; its level-`proposal_level` cell is
  * entered exactly as the plain walk would enter it (same candidates, same
@@ -396,8 +397,13 @@ int qbc_load_flat(qbc_ctx* ctx, int tree, const char* pnt_path, const char* col_
  * Autotuner (not part of the reference). Times frames of these views
  * (device outputs, these render options) on the context's stream under
  * candidate tuning options, one option after another with the others kept
- * at their best so far: the service threshold (1..16), the warp tile width
- * (2, 4, 8, 16, 32) and the render blocks per SM (0, 2..8). Each candidate gets
+ * at their best so far. With QBC_PROPOSE_MLP first the network's proposals:
+ * the gate (1000 = off, 900, 700, 500, 300, 0 per mille), then, unless off,
+ * the proposal count (1..3) and, when opts->proposal_level is 0, the cell
+ * level (5..8), so that a network whose tries cost more than they save is
+ * switched off and the frame is never slower than the plain two-pass
+ * frame; then the service threshold (1..16), the warp tile width (2, 4, 8,
+ * 16, 32) and the render blocks per SM (0, 2..8). Each candidate gets
  * one untimed frame, then `reps` (1..101) frames timed with CUDA events; its
  * time is their median. The fastest setting stays set on the context (the
  * initial one on error). The options change only the time of a frame, never
@@ -411,6 +417,10 @@ typedef struct qbc_tune_result
     int32_t candidates;  /* settings timed */
     float   ms_initial;  /* median frame time under the options found */
     float   ms_best;     /* ... under the options left set */
+    int32_t proposal_gate;  /* QBC_PROPOSE_MLP frames: gate left set (1000: proposals off) */
+    int32_t proposal_count;
+    int32_t proposal_level;
+    int32_t pad;
 } qbc_tune_result;
 
 int qbc_autotune(qbc_ctx* ctx, const qbc_view* views, const qbc_outputs* dev_outs, int n, const qbc_render_opts* opts, int reps, qbc_tune_result* result);
@@ -507,9 +517,12 @@ int qbc_synchronize(qbc_ctx* ctx);
  *   QBC_OPT_SERVICE_MIN  1..32, default 4: in the persistent render kernel a
  *   lane whose ray ended waits until this many lanes of its warp wait (or no
  *   ray runs) before the warp starts their next rays together.
- *   QBC_OPT_PROPOSAL_GATE  0..999 per mille, default 500: QBC_PROPOSE_MLP
+ *   QBC_OPT_PROPOSAL_GATE  0..1000 per mille, default 500: QBC_PROPOSE_MLP
  *   tries a pixel's proposals only when the network's occlusion probability
- *   is at least this (0: always).
+ *   is at least this (0: always; 1000: never, and the network is not run:
+ *   the frame is the plain two-pass frame).
+ *   QBC_OPT_PROPOSAL_LEVEL  1..QBC_MAX_LEVEL, default 8: level of the
+ *   proposed cells when a render's opts->proposal_level is 0.
  *   QBC_OPT_PROPOSAL_COUNT  1..3, default 3: network proposals tried per
  *   pixel, earliest first.
  *   QBC_OPT_BOX_PRUNE  1 (default) or 0: the walk skips a child whose
@@ -536,6 +549,7 @@ int qbc_synchronize(qbc_ctx* ctx);
 #define QBC_OPT_PROPOSAL_COUNT 5
 #define QBC_OPT_BOX_PRUNE 6
 #define QBC_OPT_PERSISTENT 7
+#define QBC_OPT_PROPOSAL_LEVEL 8
 int qbc_set_option(qbc_ctx* ctx, int option, int value);
 int qbc_get_option(qbc_ctx* ctx, int option, int* value);
 

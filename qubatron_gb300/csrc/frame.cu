@@ -34,6 +34,7 @@ struct FrameSignature {
   int32_t blocks_per_sm;
   int32_t proposal_count;
   int32_t persistent;
+  int32_t proposal_level;
 };
 
 bool same_signature(const FrameSignature& a, const FrameSignature& b) {
@@ -47,7 +48,8 @@ bool same_signature(const FrameSignature& a, const FrameSignature& b) {
   return a.rec == b.rec && a.rec_cap == b.rec_cap && a.pixlog == b.pixlog && a.pixlog_cap == b.pixlog_cap &&
          a.net_w == b.net_w && a.net_b == b.net_b && a.stream == b.stream && a.service_min == b.service_min &&
          a.proposal_gate == b.proposal_gate && a.tile_shift == b.tile_shift && a.blocks_per_sm == b.blocks_per_sm &&
-         a.proposal_count == b.proposal_count && a.persistent == b.persistent;
+         a.proposal_count == b.proposal_count && a.persistent == b.persistent &&
+         a.proposal_level == b.proposal_level;
 }
 
 FrameSignature frame_signature(const qbc_ctx* c) {
@@ -66,6 +68,7 @@ FrameSignature frame_signature(const qbc_ctx* c) {
   f.blocks_per_sm = c->blocks_per_sm;
   f.proposal_count = c->proposal_count;
   f.persistent = c->persistent;
+  f.proposal_level = c->proposal_level;
   return f;
 }
 
@@ -262,9 +265,25 @@ extern "C" int qbc_graph_destroy(qbc_graph* g) {
 
 namespace {
 
+// A tuning setting: warp tile, blocks per SM, service threshold, and for
+// frames with network proposals the gate (1000: off), count and cell level.
 struct TuneSetting {
   int shift, blocks, service;
+  int gate, count, level;
 };
+
+TuneSetting current_setting(const qbc_ctx* c) {
+  return {c->tile_shift, c->blocks_per_sm, c->service_min, c->proposal_gate, c->proposal_count, c->proposal_level};
+}
+
+void apply_setting(qbc_ctx* c, const TuneSetting& s) {
+  c->tile_shift = s.shift;
+  c->blocks_per_sm = s.blocks;
+  c->service_min = s.service;
+  c->proposal_gate = s.gate;
+  c->proposal_count = s.count;
+  c->proposal_level = s.level;
+}
 
 // Median device time of `reps` frames (after one untimed frame).
 int time_frames(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs, int n, const qbc_render_opts* opts,
@@ -287,18 +306,13 @@ int time_frames(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs, int 
 
 int autotune_impl(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs, int n, const qbc_render_opts* opts,
                   int reps, cudaEvent_t* ev, TuneSetting* best, qbc_tune_result* res) {
-  auto apply = [c](const TuneSetting& s) {
-    c->tile_shift = s.shift;
-    c->blocks_per_sm = s.blocks;
-    c->service_min = s.service;
-  };
   float best_ms = 0.0f;
   int rc = time_frames(c, views, outs, n, opts, reps, ev, &best_ms);
   if (rc) return rc;
   res->ms_initial = best_ms;
   res->candidates = 1;
   auto consider = [&](const TuneSetting& s) -> int {
-    apply(s);
+    apply_setting(c, s);
     float ms = 0.0f;
     int e = time_frames(c, views, outs, n, opts, reps, ev, &ms);
     if (e) return e;
@@ -309,13 +323,38 @@ int autotune_impl(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs, in
     }
     return QBC_OK;
   };
-  // one option at a time, each kept at its best before the next is swept
+  // network proposals first: whether they pay at all (gate 1000 is off),
+  // how confident the network must be, how many to try, at which level
+  if (opts && opts->proposals == QBC_PROPOSE_MLP) {
+    for (int g : {1000, 900, 700, 500, 300, 0})
+      if (g != best->gate && (rc = consider({best->shift, best->blocks, best->service, g, best->count, best->level})))
+        return rc;
+    if (best->gate < 1000) {
+      for (int k : {1, 2, 3})
+        if (k != best->count &&
+            (rc = consider({best->shift, best->blocks, best->service, best->gate, k, best->level})))
+          return rc;
+      if (opts->proposal_level == 0)
+        for (int l : {5, 6, 7, 8})
+          if (l != best->level &&
+              (rc = consider({best->shift, best->blocks, best->service, best->gate, best->count, l})))
+            return rc;
+    }
+  }
+  // then the schedule, one option at a time, each kept at its best before
+  // the next is swept
   for (int sm : {1, 2, 3, 4, 6, 8, 12, 16})
-    if (sm != best->service && (rc = consider({best->shift, best->blocks, sm}))) return rc;
+    if (sm != best->service &&
+        (rc = consider({best->shift, best->blocks, sm, best->gate, best->count, best->level})))
+      return rc;
   for (int sh : {1, 2, 3, 4, 5})
-    if (sh != best->shift && (rc = consider({sh, best->blocks, best->service}))) return rc;
+    if (sh != best->shift &&
+        (rc = consider({sh, best->blocks, best->service, best->gate, best->count, best->level})))
+      return rc;
   for (int bl : {0, 2, 3, 4, 6, 8})
-    if (bl != best->blocks && (rc = consider({best->shift, bl, best->service}))) return rc;
+    if (bl != best->blocks &&
+        (rc = consider({best->shift, bl, best->service, best->gate, best->count, best->level})))
+      return rc;
   res->ms_best = best_ms;
   return QBC_OK;
 }
@@ -337,18 +376,19 @@ extern "C" int qbc_autotune(qbc_ctx* c, const qbc_view* views, const qbc_outputs
     cudaEventDestroy(ev[0]);
     return fail(QBC_E_CUDA, "qbc_autotune: event");
   }
-  const TuneSetting initial{c->tile_shift, c->blocks_per_sm, c->service_min};
+  const TuneSetting initial = current_setting(c);
   TuneSetting best = initial;
   rc = autotune_impl(c, views, dev_outs, n, opts, reps, ev, &best, result);
   const TuneSetting keep = rc ? initial : best;
-  c->tile_shift = keep.shift;
-  c->blocks_per_sm = keep.blocks;
-  c->service_min = keep.service;
+  apply_setting(c, keep);
   cudaEventDestroy(ev[0]);
   cudaEventDestroy(ev[1]);
   if (rc) return rc;
   result->tile_width = 1 << keep.shift;
   result->blocks_per_sm = keep.blocks;
   result->service_min = keep.service;
+  result->proposal_gate = keep.gate;
+  result->proposal_count = keep.count;
+  result->proposal_level = keep.level;
   return QBC_OK;
 }

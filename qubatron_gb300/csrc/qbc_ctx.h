@@ -77,6 +77,7 @@ struct qbc_ctx {
   int blocks_per_sm = 0;  // render blocks per SM (0: as many as fit)
   int proposal_gate = 500;  // per mille: minimum predicted occlusion probability to try a proposal
   int proposal_count = 3;   // network proposals tried per pixel (earliest first)
+  int proposal_level = 8;   // level of the proposed cells when a render's options leave it 0
   int box_prune = 1;        // skip subtrees whose leaf boxes the ray misses
   int persistent = 1;       // fused frames on the persistent kernel (0: one thread per pixel)
   int64_t launches = 0;

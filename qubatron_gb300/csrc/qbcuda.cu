@@ -124,8 +124,14 @@ extern "C" int qbc_set_option(qbc_ctx* c, int option, int value) {
     return QBC_OK;
   }
   if (option == QBC_OPT_PROPOSAL_GATE) {
-    if (value < 0 || value > 999) return fail(QBC_E_ARG, "qbc_set_option: proposal gate %d outside 0..999", value);
+    if (value < 0 || value > 1000) return fail(QBC_E_ARG, "qbc_set_option: proposal gate %d outside 0..1000", value);
     c->proposal_gate = value;
+    return QBC_OK;
+  }
+  if (option == QBC_OPT_PROPOSAL_LEVEL) {
+    if (value < 1 || value > QBC_MAX_LEVEL)
+      return fail(QBC_E_ARG, "qbc_set_option: proposal level %d outside 1..%d", value, QBC_MAX_LEVEL);
+    c->proposal_level = value;
     return QBC_OK;
   }
   if (option == QBC_OPT_PROPOSAL_COUNT) {
@@ -169,6 +175,10 @@ extern "C" int qbc_get_option(qbc_ctx* c, int option, int* value) {
   }
   if (option == QBC_OPT_PROPOSAL_COUNT) {
     *value = c->proposal_count;
+    return QBC_OK;
+  }
+  if (option == QBC_OPT_PROPOSAL_LEVEL) {
+    *value = c->proposal_level;
     return QBC_OK;
   }
   if (option == QBC_OPT_BOX_PRUNE) {
@@ -897,8 +907,11 @@ int launch_modes(qbc_ctx* c, const qbc::Batch& b, size_t smem, const qbc_render_
   w.stats = c->wstats;
   w.cap = (uint32_t)std::min<int64_t>(c->rec_cap, 0xFFFFFFFFll);
   w.log = opts->log ? 1 : 0;
-  w.nprop = opts->proposals != QBC_PROPOSE_NONE ? 3 : 0;
-  w.pdepth = opts->proposal_level > 0 ? opts->proposal_level : 8;
+  // a gate of 1000 switches the network's proposals off: no inference, the
+  // plain shade pass
+  const bool mlp_off = opts->proposals == QBC_PROPOSE_MLP && c->proposal_gate >= 1000;
+  w.nprop = (opts->proposals != QBC_PROPOSE_NONE && !mlp_off) ? 3 : 0;
+  w.pdepth = opts->proposal_level > 0 ? opts->proposal_level : c->proposal_level;
   w.pixlog = opts->log ? c->pixlog : nullptr;
   QBC_CUDA(cudaMemsetAsync(c->wcount, 0, 2 * sizeof(unsigned int), c->stream));
   int rc = launch_render<EXACT, DYN, qbc::kPrimaryPass, false>(c, b, smem, w);
@@ -913,7 +926,7 @@ int launch_modes(qbc_ctx* c, const qbc::Batch& b, size_t smem, const qbc_render_
     qbc::fill_random_proposals<<<c->sm_count * 8, 256, 0, c->stream>>>(w, (unsigned long long)opts->seed);
     QBC_CUDA(cudaGetLastError());
     ++c->launches;
-  } else if (opts->proposals == QBC_PROPOSE_MLP) {
+  } else if (opts->proposals == QBC_PROPOSE_MLP && !mlp_off) {
     rc = propose_mlp(c, b, w);
     if (rc) return rc;
   }

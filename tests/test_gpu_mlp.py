@@ -101,8 +101,36 @@ def test_train_then_propose(ctx):
             _check_exact(plain, got, stats)
             tried[gate, level] = stats["proposals_tried"]
     assert tried[0, 8] > 0 and tried[500, 8] <= tried[0, 8], tried
+    # gate 1000: the network is not run, the frame is the plain two-pass one
+    ctx.set_option(L.OPT_PROPOSAL_GATE, 1000)
+    got, stats = ctx.render_host_ex(held, ALL, two_pass=True, proposals=L.PROPOSE_MLP)
+    assert stats["proposals_tried"] == 0 and _check_exact(plain, got, stats) == 0
+    # the context's level applies when the render leaves it 0
+    ctx.set_option(L.OPT_PROPOSAL_GATE, 0)
+    ctx.set_option(L.OPT_PROPOSAL_LEVEL, 5)
+    got, st5 = ctx.render_host_ex(held, ALL, two_pass=True, proposals=L.PROPOSE_MLP)
+    _check_exact(plain, got, st5)
+    assert st5["proposals_tried"] == tried[0, 5], (st5, tried)
+    # the autotuner sweeps the gate (off included), count and level, and
+    # leaves a setting whose pixels are the plain ones
+    import torch
+    import qubatron_gb300 as qb
+    frames = [torch.empty((v.height_px, v.width_px, 4), dtype=torch.uint8, device="cuda") for v in held]
+    outs = []
+    for f in frames:
+        o = qb.Outputs()
+        o.rgba8 = f.data_ptr()
+        outs.append(o)
+    r = ctx.autotune(held, outs, reps=1, two_pass=True, proposals=L.PROPOSE_MLP)
+    assert r["proposal_gate"] in (1000, 900, 700, 500, 300, 0) and 1 <= r["proposal_count"] <= 3
+    assert r["proposal_level"] in (5, 6, 7, 8) and r["candidates"] >= 20, r
+    assert ctx.get_option(L.OPT_PROPOSAL_GATE) == r["proposal_gate"]
+    got, stats = ctx.render_host_ex(held, ALL, two_pass=True, proposals=L.PROPOSE_MLP)
+    _check_exact(plain, got, stats)
     with pytest.raises(QbcError):
-        ctx.set_option(L.OPT_PROPOSAL_GATE, 1000)
+        ctx.set_option(L.OPT_PROPOSAL_GATE, 1001)
+    with pytest.raises(QbcError):
+        ctx.set_option(L.OPT_PROPOSAL_LEVEL, 0)
     ctx.proposal_clear()
     with pytest.raises(QbcError):
         ctx.proposal_train(steps=1)
