@@ -537,6 +537,66 @@ def proposal_comparison(args, device: int, stream, flush) -> dict:
     return out
 
 
+def proposal_sweep(ctx, qb, views, outs, stream, update, args):
+    """Where the network's proposals could pay and why they do not: per cell
+    level, gate and proposal count, the tries, proofs, hit rate, node visits
+    per try (the cost of a failed try) against the plain shadow-walk visits a
+    proof avoids, and the eager two-pass frame time; and the same for perfect
+    proposals (the first leaf a logged plain render of the same frame found),
+    the ceiling of any exact proposal. One frame (the first timed pose of
+    the character, when there is one)."""
+    import torch
+    lib = qb._lib
+    update(args.warmup)
+    keep = {o: ctx.get_option(o) for o in (lib.OPT_PROPOSAL_GATE, lib.OPT_PROPOSAL_COUNT, lib.OPT_PROPOSAL_LEVEL)}
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    def frame(kw):
+        ms = []
+        stats = None
+        for r in range(4):
+            ev[0].record(stream)
+            stats = ctx.render_views_ex(views, outs, True, **kw)
+            ev[1].record(stream)
+            torch.cuda.synchronize()
+            if r:
+                ms.append(ev[0].elapsed_time(ev[1]))
+        return stats, statistics.median(ms)
+
+    plain, plain_ms = frame({"two_pass": True})
+    rows = []
+
+    def row(source, gate, count, level, st, ms):
+        tried, proven = st["proposals_tried"], st["proposals_proven"]
+        avoided = plain["shadow_visits"] - st["shadow_visits"]
+        rows.append({"source": source, "gate": gate, "count": count, "level": level, "tried": tried,
+                     "proven": proven, "hit_rate": proven / max(1, tried),
+                     "visits_per_try": st["proposal_visits"] / max(1, tried),
+                     "plain_visits_avoided_per_proof": avoided / max(1, proven),
+                     "shadow_visits_vs_plain": (st["shadow_visits"] + st["proposal_visits"])
+                     / max(1, plain["shadow_visits"]),
+                     "ms": ms, "speedup_vs_plain_two_pass": plain_ms / ms})
+
+    for level in (5, 6, 7, 8):
+        for gate in (500, 900):
+            for count in (1, 3):
+                ctx.set_option(lib.OPT_PROPOSAL_GATE, gate)
+                ctx.set_option(lib.OPT_PROPOSAL_COUNT, count)
+                ctx.set_option(lib.OPT_PROPOSAL_LEVEL, level)
+                st, ms = frame({"two_pass": True, "proposals": lib.PROPOSE_MLP})
+                row("network", gate, count, level, st, ms)
+    if len(views) <= 32:  # the render log covers one launch of views
+        ctx.render_views_ex(views, outs, True, two_pass=True, log=True)
+        for level in (5, 6, 8):
+            st, ms = frame({"two_pass": True, "proposals": lib.PROPOSE_LOGGED, "proposal_level": level})
+            row("logged (perfect)", None, 1, level, st, ms)
+    for o, v in keep.items():
+        ctx.set_option(o, v)
+    return {"plain_two_pass_ms": plain_ms, "shadow_rays": plain["shadow_rays"],
+            "shadow_visits_plain": plain["shadow_visits"], "rows": rows,
+            "timing": "eager two-pass frames, median of 3 after one untimed"}
+
+
 def run_gpu(args):
     import torch
     import qubatron_gb300 as qb
@@ -742,6 +802,9 @@ def run_gpu(args):
             "visits_saved_frac": 1.0 - vis_mlp / max(1, st_two["shadow_visits"]),
         }
 
+    if training is not None and args.proposal_sweep:
+        proposal["sweep"] = proposal_sweep(ctx, qb, views, outs, stream, update, args)
+
     # the same frames on the plain one-thread-per-pixel schedule (no
     # persistent queue, no batched ray starts), same tuning otherwise
     ctx.set_option(qb._lib.OPT_PERSISTENT, 0)
@@ -774,13 +837,17 @@ def run_gpu(args):
     hbm, peak_kind = peaks()
 
     achieved = alg_bytes / (ms / 1000.0) / 1e9
-    traffic = None
+    # DRAM traffic of the frame kernel: one ncu capture of a one-view case of
+    # the same scene (profiles/), scaled to this launch by algorithmic bytes
+    traffic, traffic_kind = None, None
     tpath = os.path.join(ROOT, "profiles", "render_kernel_traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
             t = json.load(f)
-        if t.get("workload") == WORKLOAD:
-            traffic = t.get("dram_bytes_per_launch")
+        if t.get("applies_to") == WORKLOAD:
+            traffic = t["dram_bytes_per_launch_captured"] * alg_bytes / t["algorithmic_bytes_per_launch_captured"]
+            traffic_kind = (f"ncu dram__bytes of {t['captured_on']} ({t['dram_bytes_per_launch_captured']} B), "
+                            "scaled by algorithmic bytes to this launch")
 
     line = {
         "metric": "primary+shadow Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world,
@@ -792,7 +859,7 @@ def run_gpu(args):
         "e2e": e2e,
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": traffic, "peak_kind": f"{peak_kind} (burst copy)",
+                     "traffic": traffic, "traffic_kind": traffic_kind, "peak_kind": f"{peak_kind} (burst copy)",
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "node_visits_per_launch": statistics.mean(frame_visits),
                      "box_words_per_launch": statistics.mean(frame_words)},
@@ -865,6 +932,8 @@ def main():
     ap.add_argument("--proposal-level", type=int, default=0,
                     help="octree level of the proposed cells (0: the context's, swept by the autotuner)")
     ap.add_argument("--proposal-count", type=int, default=3, help="network proposals tried per pixel (1..3)")
+    ap.add_argument("--proposal-sweep", action="store_true",
+                    help="network workloads: per level, gate and count, the proposals' hit rate and cost")
     ap.add_argument("--no-proposal-block", action="store_true",
                     help="skip the learned-vs-plain comparison on the proposal workload")
     ap.add_argument("--proposal-cpu-seconds", type=float, default=4.0,

@@ -485,7 +485,9 @@ int Net::gradient(const bf16* X, const float* tlab, const int8_t* kind, int64_t 
   ++g_launches;
   const bf16* W[4];
   for (int l = 0; l < 4; ++l) W[l] = wb + param_offset(l, false);
-  const int64_t kchunk = 4096;
+  // weight gradients reduce over the batch: 256-row K chunks give the
+  // product enough blocks (their partial sums meet in atomics)
+  const int64_t kchunk = 256;
   // layer 4: dW4 = dO^T A3, db4 = sum dO, dA3 = dO W4
   {
     Epi e{grad + param_offset(3, false), kHidden, nullptr, 0, nullptr, 0, nullptr, 0, 1, err};

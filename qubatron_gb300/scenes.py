@@ -212,6 +212,9 @@ WORKLOADS = {
     "floor1m_640x480": Workload("floor1m_640x480", "floor1m", 640, 480, [FLOOR_POSE]),
     "room20m_1920x1080x16": Workload("room20m_1920x1080x16", "room20m", 1920, 1080, spline_poses(1002, 16)),
     "room5m_1920x1080x1": Workload("room5m_1920x1080x1", "room5m", 1920, 1080, spline_poses(1002, 16)[:1]),
+    # the first view of the room20m batch alone: a counter-capture case of
+    # the bench's scene (its DRAM traffic is scaled to the 16-view launch)
+    "room20m_1920x1080x1": Workload("room20m_1920x1080x1", "room20m", 1920, 1080, spline_poses(1002, 16)[:1]),
 }
 _b64_sizes, _b64_poses = batch_views(64, 64)
 WORKLOADS["floor1m_char2m_mixed_x64"] = Workload("floor1m_char2m_mixed_x64", "floor1m", 0, 0, _b64_poses,
