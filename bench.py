@@ -537,6 +537,29 @@ def proposal_comparison(args, device: int, stream, flush) -> dict:
     return out
 
 
+def flare_borderline(ctx, views, ulps: int = 2) -> dict:
+    """Pixels whose flare test (acos(cos) < 0.02, evaluated as cos above the
+    largest float not above cos(0.02)) sits within `ulps` floats of its
+    threshold, over every pixel of the views, from the kernels' own camera
+    rays: the pixels where a GL driver's acos could decide otherwise."""
+    import torch
+    within = near = 0
+    for v in views:
+        n = v.width_px * v.height_px
+        idx = torch.arange(n, dtype=torch.int32, device="cuda")
+        px = (idx % v.width_px).contiguous()
+        py = (idx // v.width_px).contiguous()
+        out = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+        ctx.camera_rays_device(v, px.data_ptr(), py.data_ptr(), n, out.data_ptr())
+        torch.cuda.synchronize()
+        cosv = out[:, 3].contiguous()
+        thr = torch.tensor([v.flare_cos], dtype=torch.float32, device="cuda")
+        within += int(((cosv > thr) & (cosv <= 1.0)).sum().item())
+        d = (cosv.view(torch.int32).to(torch.int64) - thr.view(torch.int32).to(torch.int64)).abs()
+        near += int((d <= ulps).sum().item())
+    return {"pixels_in_flare_cone": within, "borderline_pixels": near, "ulps": ulps}
+
+
 def proposal_sweep(ctx, qb, views, outs, stream, update, args):
     """Where the network's proposals could pay and why they do not: per cell
     level, gate and proposal count, the tries, proofs, hit rate, node visits
@@ -867,6 +890,7 @@ def run_gpu(args):
         "step_ms": [round(x, 4) for x in step_ms],
     }
     line["plain_simple"] = plain_simple
+    line["flare_test"] = flare_borderline(ctx, views)
     if proposal is not None:
         line["run"]["per_step"] = "two-pass render with occluder-network proposals (network evaluated every step)"
         line["proposal"] = proposal

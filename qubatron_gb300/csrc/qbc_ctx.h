@@ -85,6 +85,8 @@ struct qbc_ctx {
   void* build_input = nullptr;   // device copy of host build input
   int64_t build_input_cap = 0;   // bytes
   unsigned* derr = nullptr;      // device: qbc::DeviceError bits of kernels' input checks
+  cudaStream_t copy = nullptr;   // host-output copies, overlapped with the next views' render
+  std::vector<cudaEvent_t> copy_ev;  // one per chunk of a host-output render
   int32_t* counts = nullptr;     // device: node counts of GPU-built trees (one per tree)
 };
 

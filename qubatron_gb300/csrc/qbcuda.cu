@@ -61,10 +61,12 @@ extern "C" int qbc_create(int device, qbc_ctx** out) {
   if (e == cudaSuccess) e = cudaMalloc(&c->queue, sizeof(unsigned int));
   if (e == cudaSuccess) e = cudaMalloc(&c->wcount, 2 * sizeof(unsigned int));
   if (e == cudaSuccess) e = cudaMalloc(&c->wstats, qbc::kStatCount * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc(&c->derr, sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMemset(c->derr, 0, sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMalloc(&c->counts, 2 * sizeof(int32_t));
   if (e != cudaSuccess) {
+    if (c->copy) cudaStreamDestroy(c->copy);
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
     return cuda_fail(e, "qbc_create");
@@ -101,6 +103,8 @@ extern "C" int qbc_destroy(qbc_ctx* c) {
   cudaFree(c->wcount);
   cudaFree(c->wstats);
   cudaFree(c->pixlog);
+  for (cudaEvent_t ev : c->copy_ev) cudaEventDestroy(ev);
+  if (c->copy) cudaStreamDestroy(c->copy);
   qbc::build_release(&c->build);
   cudaFree(c->build_input);
   cudaFree(c->derr);
@@ -1056,19 +1060,46 @@ int render_views_impl(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs
       off += (px * kOutBytes[k] + 255) & ~size_t(255);
     }
   }
-  for (int a = 0; a < n; a += qbc::kMaxViewsPerLaunch) {
-    int rc = launch_batch(c, views + a, dev.data() + a, std::min(qbc::kMaxViewsPerLaunch, n - a), opts);
-    if (rc) return rc;
-  }
-  for (int i = 0; i < n; ++i) {
-    size_t px = (size_t)views[i].width_px * views[i].height_px;
-    qbc_outputs h = outs[i];
-    for (int k = 0; k < 6; ++k) {
-      void* dst = *out_slot(h, k);
-      if (!dst) continue;
-      QBC_CUDA(cudaMemcpyAsync(dst, *out_slot(dev[i], k), px * kOutBytes[k], cudaMemcpyDeviceToHost, c->stream));
+  // Views in chunks of about a quarter of the pixels (at least 16M pixels,
+  // at most one launch's views): a chunk's copies to the host run on the
+  // copy stream while the next chunk renders. Each extra launch costs a
+  // tail, so small frames stay whole (16 x 1080p: 2 chunks; 32 x 4K: 4). A
+  // logged render stays one launch (its log indexes the pixels of one
+  // launch).
+  int64_t total_px = 0;
+  for (int i = 0; i < n; ++i) total_px += (int64_t)views[i].width_px * views[i].height_px;
+  const bool logged = opts && (opts->log || opts->proposals == QBC_PROPOSE_LOGGED);
+  const int64_t target = logged ? INT64_MAX : std::max<int64_t>(total_px / 4, int64_t(16) << 20);
+  int chunk = 0;
+  for (int a = 0; a < n;) {
+    int m = 0;
+    int64_t px_chunk = 0;
+    while (a + m < n && m < qbc::kMaxViewsPerLaunch && (m == 0 || px_chunk < target)) {
+      px_chunk += (int64_t)views[a + m].width_px * views[a + m].height_px;
+      ++m;
     }
+    int rc = launch_batch(c, views + a, dev.data() + a, m, opts);
+    if (rc) return rc;
+    if ((int)c->copy_ev.size() <= chunk) {
+      cudaEvent_t ev = nullptr;
+      QBC_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+      c->copy_ev.push_back(ev);
+    }
+    QBC_CUDA(cudaEventRecord(c->copy_ev[(size_t)chunk], c->stream));
+    QBC_CUDA(cudaStreamWaitEvent(c->copy, c->copy_ev[(size_t)chunk], 0));
+    for (int i = a; i < a + m; ++i) {
+      size_t px = (size_t)views[i].width_px * views[i].height_px;
+      qbc_outputs h = outs[i];
+      for (int k = 0; k < 6; ++k) {
+        void* dst = *out_slot(h, k);
+        if (!dst) continue;
+        QBC_CUDA(cudaMemcpyAsync(dst, *out_slot(dev[i], k), px * kOutBytes[k], cudaMemcpyDeviceToHost, c->copy));
+      }
+    }
+    a += m;
+    ++chunk;
   }
+  QBC_CUDA(cudaStreamSynchronize(c->copy));
   QBC_CUDA(cudaStreamSynchronize(c->stream));
   return read_stats(c, stats, two);
 }

@@ -260,6 +260,11 @@ class OctreeGLC:
                                         C.c_void_p(py.ctypes.data), px.size, C.c_void_p(out.ctypes.data), 0))
         return out
 
+    def camera_rays_device(self, view: View, px_ptr: int, py_ptr: int, n: int, out_ptr: int) -> None:
+        """qbc_camera_rays on device arrays (int32 px, py; float4 out)."""
+        check(self._lib.qbc_camera_rays(self.handle, C.byref(view), C.c_void_p(px_ptr), C.c_void_p(py_ptr), int(n),
+                                        C.c_void_p(out_ptr), 1))
+
     def set_stream(self, stream_ptr: Optional[int]) -> None:
         check(self._lib.qbc_set_stream(self.handle, C.c_void_p(stream_ptr or 0)))
 

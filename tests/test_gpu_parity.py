@@ -290,3 +290,36 @@ def test_camera_rays_match_mt_quat(lib, oracle, ctx):
                                       err_msg=f"camera {vi}")
         ref = oracle.camera_rays(_view_for_oracle(oracle, v), g["px"][m], g["py"][m])
         np.testing.assert_array_equal(got.view(np.uint32), ref.view(np.uint32), err_msg=f"camera {vi} cosine")
+
+
+def test_host_outputs_in_chunks_equal_device_outputs(lib, ctx, floor50k_scene):
+    """A host-output render of more than 16M pixels is rendered in chunks of
+    views whose copies to the host overlap the next chunk's render; every
+    stream must equal the device-output render of the same views."""
+    import torch
+
+    import qubatron_gb300 as qb
+    from qubatron_gb300 import view_setup
+    s = floor50k_scene
+    upload_scene(ctx, s.nodes, s.colors, s.normals)
+    views = [view_setup(1920, 1080, (903.7 - 40 * k, 421.3, 1702.9), (0.1 * k - 0.2, -0.3, 0.0), 0.2 * k, 10,
+                        LEVELS, S, 0, 0.0) for k in range(12)]
+    host = ctx.render_host(views, ("rgba8", "flags", "leaf"))
+    dev, outs = [], []
+    for v in views:
+        t = {"rgba8": torch.empty((v.height_px, v.width_px, 4), dtype=torch.uint8, device="cuda"),
+             "flags": torch.empty((v.height_px, v.width_px), dtype=torch.int32, device="cuda"),
+             "leaf": torch.empty((v.height_px, v.width_px, 4), dtype=torch.int32, device="cuda")}
+        o = qb.Outputs()
+        o.rgba8, o.flags, o.leaf = t["rgba8"].data_ptr(), t["flags"].data_ptr(), t["leaf"].data_ptr()
+        dev.append(t)
+        outs.append(o)
+    ctx.render_views(views, outs, on_device=True)
+    ctx.synchronize()
+    hits = 0
+    for h, d in zip(host, dev):
+        assert np.array_equal(h["rgba8"], d["rgba8"].cpu().numpy())
+        assert np.array_equal(h["flags"], d["flags"].cpu().numpy().view(np.uint32))
+        assert np.array_equal(h["leaf"], d["leaf"].cpu().numpy())
+        hits += int((h["flags"] & 1).sum())
+    assert hits > 100_000
