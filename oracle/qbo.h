@@ -131,6 +131,11 @@ void qbo_trace(const qbo_scene* sc, const float basecube[4], int maxlevel, const
 /* One fragment: main() (octree_fsh.c:399-464) at pixel (i, j), j from the bottom. */
 void qbo_shade_pixel(const qbo_scene* sc, const qbo_view* v, int i, int j, float rgba[4], uint32_t* flags, int32_t leaf[4], float isp[4], uint32_t visits[4]);
 
+/* Shading of a primary hit (octree_fsh.c:431-449): col (the hit texel,
+ * alpha kept) is shaded in place; sqr is the squared distance from the
+ * shadow ray's first leaf to the hit. */
+void qbo_shade(const float isp[3], const float nrm[3], const float csv[3], const float light[3], float sqr, int shoot, float col[4]);
+
 /* Camera ray of pixel (i, j) (octree_fsh.c:401-418): out = (csv, cosine of
  * the angle between csv and light - camfp). */
 void qbo_camera_ray(const qbo_view* v, int i, int j, float out[4]);

@@ -130,6 +130,8 @@ def qbo() -> C.CDLL:
         lib.qbo_scene_generate.restype = C.c_int
         lib.qbo_camera_ray.argtypes = [C.POINTER(QboView), C.c_int, C.c_int, f32p]
         lib.qbo_camera_ray.restype = None
+        lib.qbo_shade.argtypes = [f32p, f32p, f32p, f32p, C.c_float, C.c_int, f32p]
+        lib.qbo_shade.restype = None
         _qbo = lib
     return _qbo
 
@@ -160,6 +162,8 @@ def ref() -> C.CDLL | None:
         lib.qbref_frame_quats.restype = None
         lib.qbref_camera_dirs.argtypes = [f32p, f32p, f32p, f32p, C.c_long, f32p]
         lib.qbref_camera_dirs.restype = None
+        lib.qbref_shade.argtypes = [f32p, f32p, f32p, f32p, C.c_float, C.c_int, f32p]
+        lib.qbref_shade.restype = None
         _ref = lib
     return _ref
 
@@ -375,4 +379,19 @@ def ref_camera_dirs(qz, qx, cfp, ctp) -> np.ndarray:
     out = np.zeros((ctp.shape[0], 3), np.float32)
     ref().qbref_camera_dirs(qz.ctypes.data_as(f32p), qx.ctypes.data_as(f32p), cfp.ctypes.data_as(f32p),
                             ctp.ctypes.data_as(f32p), ctp.shape[0], out.ctypes.data_as(f32p))
+    return out
+
+
+def shade(isp, nrm, csv, light, sqr, shoot, col, reference: bool = False) -> np.ndarray:
+    """Shading of hits (octree_fsh.c:431-449), rows of isp, nrm, csv (3),
+    col (4), sqr: the oracle's restatement, or (reference=True) the same
+    formula on the reference's own C vector helpers."""
+    isp, nrm, csv = (np.ascontiguousarray(a, np.float32).reshape(-1, 3) for a in (isp, nrm, csv))
+    out = np.ascontiguousarray(col, np.float32).reshape(-1, 4).copy()
+    light = np.ascontiguousarray(light, np.float32)
+    sqr = np.asarray(sqr, np.float32).ravel()
+    fn = ref().qbref_shade if reference else qbo().qbo_shade
+    for k in range(isp.shape[0]):
+        fn(isp[k].ctypes.data_as(f32p), nrm[k].ctypes.data_as(f32p), csv[k].ctypes.data_as(f32p),
+           light.ctypes.data_as(f32p), float(sqr[k]), int(shoot), out[k].ctypes.data_as(f32p))
     return out

@@ -467,6 +467,31 @@ void qbo_view_setup(float width, float height, const float position[3], const fl
     v->shoot    = shoot;
 }
 
+void qbo_shade(const float isp[3], const float nrm[3], const float csv[3], const float light[3], float sqr, int shoot, float col[4])
+{
+    /* octree_fsh.c:431-449 */
+    float lghtv[3] = {isp[0] - light[0], isp[1] - light[1], isp[2] - light[2]};
+    float nl[3], nn[3], nc[3];
+    float neg_l[3] = {-lghtv[0], -lghtv[1], -lghtv[2]};
+    float neg_c[3] = {-csv[0], -csv[1], -csv[2]};
+    normalize3(neg_l, nl);
+    normalize3(nrm, nn);
+    normalize3(neg_c, nc);
+    float lght_nrm_ang = glsl_max(dot3(nl, nn), 0.0f);
+    float camv_nrm_ang = glsl_max(dot3(nc, nn), 0.0f);
+
+    float lit = (15.0f < sqr) ? 0.0f : 1.0f; /* step(sqr, 15.0) */
+    float k   = 0.1f + 0.2f * camv_nrm_ang + lght_nrm_ang * lit * 0.7f;
+    col[0]    = col[0] * k;
+    col[1]    = col[1] * k;
+    col[2]    = col[2] * k;
+    col[2] *= 0.7f;
+    float g = (float) shoot * camv_nrm_ang * 0.1f;
+    col[0] += g;
+    col[1] += g;
+    col[2] += g;
+}
+
 void qbo_camera_ray(const qbo_view* v, int i, int j, float out[4])
 {
     /* ray generation (octree_fsh.c:402-413); coord is the pixel centre */
@@ -546,27 +571,8 @@ void qbo_shade_pixel(const qbo_scene* sc, const qbo_view* v, int i, int j, float
         float ispv[3] = {lc.isp[0] - res.isp[0], lc.isp[1] - res.isp[1], lc.isp[2] - res.isp[2]};
         float sqr     = ispv[0] * ispv[0] + ispv[1] * ispv[1] + ispv[2] * ispv[2];
 
-        float nl[3], nn[3], nc[3];
-        float neg_l[3] = {-lghtv[0], -lghtv[1], -lghtv[2]};
-        float neg_c[3] = {-csv[0], -csv[1], -csv[2]};
-        normalize3(neg_l, nl);
-        normalize3(res.nrm, nn);
-        normalize3(neg_c, nc);
-        float lght_nrm_ang = glsl_max(dot3(nl, nn), 0.0f);
-        float camv_nrm_ang = glsl_max(dot3(nc, nn), 0.0f);
-
-        float lit = (15.0f < sqr) ? 0.0f : 1.0f; /* step(sqr, 15.0) */
-        if (lit != 0.0f) f |= QBO_PX_LIT;
-
-        float k = 0.1f + 0.2f * camv_nrm_ang + lght_nrm_ang * lit * 0.7f;
-        col[0]  = col[0] * k;
-        col[1]  = col[1] * k;
-        col[2]  = col[2] * k;
-        col[2] *= 0.7f;
-        float g = (float) v->shoot * camv_nrm_ang * 0.1f;
-        col[0] += g;
-        col[1] += g;
-        col[2] += g;
+        if (!(15.0f < sqr)) f |= QBO_PX_LIT; /* step(sqr, 15.0) */
+        qbo_shade(res.isp, res.nrm, csv, v->light, sqr, v->shoot, col);
     }
 
     if (flare)

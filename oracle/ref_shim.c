@@ -128,3 +128,27 @@ void qbref_camera_dirs(const float* qz, const float* qx, const float* cfp, const
         out[3 * i + 2] = csv.z;
     }
 }
+
+/* The shading of octree_fsh.c:431-449 written with the reference's own C
+ * vector helpers (mt_vector_3d.c: v3_sub, v3_scale, v3_normalize, v3_dot).
+ * v3_normalize multiplies by 1 / sqrt where the shader restatement divides,
+ * so this twin agrees with it to within a few ulps, not bit for bit; it pins
+ * the formula. col is shaded in place. */
+void qbref_shade(const float* isp, const float* nrm, const float* csv, const float* light, float sqr, int shoot, float* col)
+{
+    v3_t  ispv  = {isp[0], isp[1], isp[2]};
+    v3_t  lghtv = v3_sub(ispv, (v3_t){light[0], light[1], light[2]});
+    v3_t  n     = v3_normalize((v3_t){nrm[0], nrm[1], nrm[2]});
+    float lght  = v3_dot(v3_normalize(v3_scale(lghtv, -1.0f)), n);
+    float camv  = v3_dot(v3_normalize(v3_scale((v3_t){csv[0], csv[1], csv[2]}, -1.0f)), n);
+    float lght_nrm_ang = lght > 0.0f ? lght : 0.0f;
+    float camv_nrm_ang = camv > 0.0f ? camv : 0.0f;
+    float lit = 15.0f < sqr ? 0.0f : 1.0f; /* step(sqr, 15.0) */
+    float k   = 0.1f + 0.2f * camv_nrm_ang + lght_nrm_ang * lit * 0.7f;
+    v3_t  c   = v3_scale((v3_t){col[0], col[1], col[2]}, k);
+    c.z *= 0.7f;
+    float g = (float) shoot * camv_nrm_ang * 0.1f;
+    col[0]  = c.x + g;
+    col[1]  = c.y + g;
+    col[2]  = c.z + g;
+}

@@ -24,6 +24,9 @@ records what that code produces:
                        after each call sequence;
 * ``camera_quat.npz``  frame quaternions and per-pixel camera rays from the
                        reference's mt_quat.c (--camera-only makes just this);
+* ``shade_ref.npz``    the shading formula on the reference's own C vector
+                       helpers (mt_vector_3d.c) for seeded inputs
+                       (--shade-only makes just this);
 * ``flat/small.{pnt,col,nrm,rng}`` + ``flat_small.npz``  a 2,000-point qmc
                        flat model (7 trailing bytes after the last point, a
                        partial int after the last range) and what the
@@ -163,11 +166,38 @@ def camera_golden() -> None:
     print("camera_quat:", len(cams), "cameras,", sum(a.size for a in rows["px"]), "pixels")
 
 
+def shade_golden() -> None:
+    """shade_ref.npz: the shading of octree_fsh.c:431-449 computed with the
+    reference's own C vector helpers (src/mt_math/mt_vector_3d.c) for seeded
+    inputs in the ranges the renders produce, and edge cases (a normal facing
+    away from the light or the camera, lit and unlit, shoot on and off)."""
+    rng = np.random.default_rng(17)
+    n = 2000
+    isp = rng.uniform(0.0, S, (n, 3)).astype(np.float32)
+    nrm = rng.normal(size=(n, 3)).astype(np.float32) * rng.uniform(0.3, 2.0, (n, 1)).astype(np.float32)
+    csv = (rng.normal(size=(n, 3)) * rng.uniform(300.0, 1500.0, (n, 1))).astype(np.float32)
+    col = np.concatenate([rng.uniform(0.0, 1.0, (n, 3)), np.ones((n, 1))], 1).astype(np.float32)
+    sqr = np.where(rng.uniform(size=n) < 0.5, rng.uniform(0.0, 15.0, n), rng.uniform(15.0, 4e5, n)).astype(np.float32)
+    sqr[:8] = [0.0, 15.0, np.nextafter(np.float32(15.0), np.float32(16.0)), 14.999999, 1e-9, 16.0, 3e5, 7.5]
+    light = np.array([420.0, 200.0, 680.0], np.float32)
+    nrm[8:16] = (light - isp[8:16]) * np.float32(-1.0)  # facing away from the light
+    csv[16:24] = nrm[16:24] * np.float32(500.0)          # facing away from the camera
+    out = {}
+    for shoot in (0, 1):
+        out[f"ref_shoot{shoot}"] = qbo.shade(isp, nrm, csv, light, sqr, shoot, col, reference=True)
+    np.savez_compressed(os.path.join(HERE, "shade_ref.npz"), isp=isp, nrm=nrm, csv=csv, col=col, sqr=sqr,
+                        light=light, **out)
+    print("shade_ref:", n, "inputs")
+
+
 def main(root: str, only=None) -> None:
     if qbo.build_reference(root) is None:
         raise SystemExit(f"reference sources not found under {root}")
     if only == "camera":
         camera_golden()
+        return
+    if only == "shade":
+        shade_golden()
         return
 
     # ---- 5-point scene ----
@@ -243,11 +273,12 @@ def main(root: str, only=None) -> None:
     print("flat_small:", got["points"].shape[0], "points,", got["ranges"].size, "range ints")
 
     camera_golden()
+    shade_golden()
 
 
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     root = args[0] if args else qbo.REFERENCE_ROOT
     if not root:
-        raise SystemExit("usage: make_golden.py REFERENCE_ROOT [--camera-only] (or set QB_REFERENCE_ROOT)")
-    main(root, "camera" if "--camera-only" in sys.argv else None)
+        raise SystemExit("usage: make_golden.py REFERENCE_ROOT [--camera-only | --shade-only] (or set QB_REFERENCE_ROOT)")
+    main(root, "camera" if "--camera-only" in sys.argv else ("shade" if "--shade-only" in sys.argv else None))
