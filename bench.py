@@ -653,6 +653,8 @@ def run_gpu(args):
         ctx.set_option(qb._lib.OPT_TILE_WIDTH, args.tile_width)
     if args.blocks_per_sm:
         ctx.set_option(qb._lib.OPT_BLOCKS_PER_SM, args.blocks_per_sm)
+    if args.split_trees >= 0:
+        ctx.set_option(qb._lib.OPT_SPLIT_TREES, args.split_trees)
 
     def render_plain(v, o, dev):
         ctx.render_views(v, o, on_device=dev)
@@ -727,8 +729,14 @@ def run_gpu(args):
         # tuning options (service threshold, warp tile, blocks per SM) picked
         # by timing this frame; untimed
         update(0)
-        # very large frames: tune on the first views (same sizes and scene)
-        k = len(views) if sum(v.width_px * v.height_px for v in views) <= 40_000_000 else 4
+        # very large frames: tune on the first views holding ~100M pixels
+        # (same sizes and scene; enough pixels per launch that the fixed
+        # costs of a launch, e.g. a split frame's second tail, weigh as in
+        # the whole frame)
+        k, px = 0, 0
+        while k < len(views) and px < 100_000_000:
+            px += views[k].width_px * views[k].height_px
+            k += 1
         tuning = ctx.autotune(views[:k], outs[:k], reps=3, **(mlp_kw if training is not None else {}))
         tuning["views_timed"] = k
         torch.cuda.synchronize()
@@ -946,6 +954,8 @@ def main():
     ap.add_argument("--service-min", type=int, default=0, help="set the service threshold (no autotune)")
     ap.add_argument("--tile-width", type=int, default=0, help="set the warp tile width 4/8/16/32 (no autotune)")
     ap.add_argument("--blocks-per-sm", type=int, default=0, help="set render blocks per SM (no autotune)")
+    ap.add_argument("--split-trees", type=int, default=-1, choices=[-1, 0, 1],
+                    help="two-tree fused frames: 1 one-tree + two-tree launch, 0 one launch (-1: library default)")
     ap.add_argument("--workload", default=None)
     ap.add_argument("--train-steps", type=int, default=4000, help="occluder-network training steps")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",

@@ -334,7 +334,9 @@ typedef struct qbc_render_opts
 } qbc_render_opts;
 
 /* Counters of the last qbc_render_views_ex call. The first six count the
- * shade pass of a two_pass render (0 otherwise); box_words counts the 8-byte
+ * shade pass of a two_pass render (0 otherwise; in a fused frame that runs
+ * split, QBC_OPT_SPLIT_TREES, queued counts the pixels the one-tree kernel
+ * handed to the two-tree kernel); box_words counts the 8-byte
  * leaf-box words (QBC_OPT_BOX_PRUNE) read by all walks of a render in which a
  * view has a visits output (0 otherwise). */
 typedef struct qbc_render_stats
@@ -420,7 +422,7 @@ typedef struct qbc_tune_result
     int32_t proposal_gate;  /* QBC_PROPOSE_MLP frames: gate left set (1000: proposals off) */
     int32_t proposal_count;
     int32_t proposal_level;
-    int32_t pad;
+    int32_t split_trees;    /* two-tree fused frames: QBC_OPT_SPLIT_TREES left set */
 } qbc_tune_result;
 
 int qbc_autotune(qbc_ctx* ctx, const qbc_view* views, const qbc_outputs* dev_outs, int n, const qbc_render_opts* opts, int reps, qbc_tune_result* result);
@@ -541,6 +543,16 @@ int qbc_synchronize(qbc_ctx* ctx);
  *   one launch of tiles_total / 4 blocks. Same pixels; the plain schedule is
  *   the baseline the persistent kernel is measured against. Two-pass renders
  *   always run persistent.
+ *   QBC_OPT_SPLIT_TREES  0 (default) or 1: with 1, a persistent fused frame
+ *   with a dynamic tree whose leaf boxes are built (QBC_OPT_BOX_PRUNE 1,
+ *   exactly representable cubes) runs as two launches: a one-tree kernel
+ *   walks every ray that misses the leaf boxes of the dynamic root's
+ *   children and hands each pixel whose next ray may not to a two-tree
+ *   kernel, which finishes it (and, should the record queue fill, the tiles
+ *   the one-tree kernel then left). Same pixels; the queue takes 32 bytes
+ *   per pixel of the largest launch. It pays on large frames in which the
+ *   character covers little (32 4K views of a house: -8 %), not on a view
+ *   aimed at the character (+5 %); qbc_autotune decides it.
  */
 #define QBC_OPT_SERVICE_MIN 1
 #define QBC_OPT_PROPOSAL_GATE 2
@@ -550,6 +562,7 @@ int qbc_synchronize(qbc_ctx* ctx);
 #define QBC_OPT_BOX_PRUNE 6
 #define QBC_OPT_PERSISTENT 7
 #define QBC_OPT_PROPOSAL_LEVEL 8
+#define QBC_OPT_SPLIT_TREES 9
 int qbc_set_option(qbc_ctx* ctx, int option, int value);
 int qbc_get_option(qbc_ctx* ctx, int option, int* value);
 

@@ -195,6 +195,24 @@ void qbo_trace(const qbo_scene* sc, const float bc[4], int maxlevel, const float
         for (int k = 0; k < 3; ++k) inv[k] = 1.0f / dir[k];
     const float box_m = bc[3] * 6.1035156e-05f;
 
+    /* a ray that misses the leaf box of every child of the dynamic root can
+     * reach no dynamic leaf: the library walks such a ray on the static tree
+     * alone (no dynamic lookups, no dynamic visits); the pixels are the same */
+    int use_d = 1;
+    if (box_d && td->box_depth > 1)
+    {
+        qbo_box_frame_t bf0;
+        qbo_box_frame(bc, pos, inv, box_m, &bf0);
+        int near = 0;
+        for (int o = 0; o < 8; ++o)
+        {
+            int32_t dummy = 0;
+            int32_t c     = node_slot(td, 0, o, 0, &dummy);
+            if (c > 0 && qbo_box_hit(td->cbox[2 * o], td->cbox[2 * o + 1], o, &bf0)) near = 1;
+        }
+        use_d = near;
+    }
+
     for (;;)
     {
         out->steps++;
@@ -205,7 +223,7 @@ void qbo_trace(const qbo_scene* sc, const float bc[4], int maxlevel, const float
         {
             /* leaf: model indices, colour and normal (octree_fsh.c:218-247) */
             int32_t ms = node_slot(ts, L->node[0], 8, level, &out->oob);
-            int32_t md = node_slot(td, L->node[1], 8, level, &out->oob);
+            int32_t md = use_d ? node_slot(td, L->node[1], 8, level, &out->oob) : 0;
 
             out->isp[0] = L->isps[0].x;
             out->isp[1] = L->isps[0].y;
@@ -239,7 +257,8 @@ void qbo_trace(const qbo_scene* sc, const float bc[4], int maxlevel, const float
             /* a visit reads the node's child block: counted when the node
              * exists and lies inside the uploaded array */
             if (!(L->node[0] == 0 && level > 0) && L->node[0] >= 0 && L->node[0] < ts->n_nodes) out->visits[0]++;
-            if (!(L->node[1] == 0 && level > 0) && L->node[1] >= 0 && L->node[1] < td->n_nodes) out->visits[1]++;
+            if (use_d && !(L->node[1] == 0 && level > 0) && L->node[1] >= 0 && L->node[1] < td->n_nodes)
+                out->visits[1]++;
 
             v4 cb = {tlf.x + tlf.w, tlf.y - tlf.w, tlf.z - tlf.w, 0.0f};
             v4 hlf;
@@ -302,7 +321,7 @@ void qbo_trace(const qbo_scene* sc, const float bc[4], int maxlevel, const float
                 pre = oct;
 
                 int32_t cs = node_slot(ts, L->node[0], oct, level, &out->oob);
-                int32_t cd = node_slot(td, L->node[1], oct, level, &out->oob);
+                int32_t cd = use_d ? node_slot(td, L->node[1], oct, level, &out->oob) : 0;
                 int     keep = cs > 0 || cd > 0;
                 if (keep && (lev_s || lev_d))
                 {
@@ -343,7 +362,7 @@ void qbo_trace(const qbo_scene* sc, const float bc[4], int maxlevel, const float
             L->ispsi = 128 | (nxt_ind << 4) | cur_len;
 
             int32_t cs = node_slot(ts, L->node[0], nxt_oct, level, &out->oob);
-            int32_t cd = node_slot(td, L->node[1], nxt_oct, level, &out->oob);
+            int32_t cd = use_d ? node_slot(td, L->node[1], nxt_oct, level, &out->oob) : 0;
 
             if (++pushes > QBO_MAX_PUSHES)
             {

@@ -158,7 +158,7 @@ class TuneResult(C.Structure):
     _fields_ = [("tile_width", C.c_int32), ("blocks_per_sm", C.c_int32), ("service_min", C.c_int32),
                 ("candidates", C.c_int32), ("ms_initial", C.c_float), ("ms_best", C.c_float),
                 ("proposal_gate", C.c_int32), ("proposal_count", C.c_int32), ("proposal_level", C.c_int32),
-                ("pad", C.c_int32)]
+                ("split_trees", C.c_int32)]
 
     def as_dict(self) -> dict:
         return {f: (float(getattr(self, f)) if f.startswith("ms") else int(getattr(self, f))) for f, _ in self._fields_}
@@ -279,6 +279,7 @@ OPT_PROPOSAL_COUNT = 5
 OPT_BOX_PRUNE = 6
 OPT_PERSISTENT = 7
 OPT_PROPOSAL_LEVEL = 8
+OPT_SPLIT_TREES = 9
 
 
 def lib_path() -> str:

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <initializer_list>
 #include <memory>
 #include <vector>
 
@@ -35,6 +36,7 @@ struct FrameSignature {
   int32_t proposal_count;
   int32_t persistent;
   int32_t proposal_level;
+  int32_t split_trees;
 };
 
 bool same_signature(const FrameSignature& a, const FrameSignature& b) {
@@ -49,7 +51,7 @@ bool same_signature(const FrameSignature& a, const FrameSignature& b) {
          a.net_w == b.net_w && a.net_b == b.net_b && a.stream == b.stream && a.service_min == b.service_min &&
          a.proposal_gate == b.proposal_gate && a.tile_shift == b.tile_shift && a.blocks_per_sm == b.blocks_per_sm &&
          a.proposal_count == b.proposal_count && a.persistent == b.persistent &&
-         a.proposal_level == b.proposal_level;
+         a.proposal_level == b.proposal_level && a.split_trees == b.split_trees;
 }
 
 FrameSignature frame_signature(const qbc_ctx* c) {
@@ -69,6 +71,7 @@ FrameSignature frame_signature(const qbc_ctx* c) {
   f.proposal_count = c->proposal_count;
   f.persistent = c->persistent;
   f.proposal_level = c->proposal_level;
+  f.split_trees = c->split_trees;
   return f;
 }
 
@@ -265,15 +268,18 @@ extern "C" int qbc_graph_destroy(qbc_graph* g) {
 
 namespace {
 
-// A tuning setting: warp tile, blocks per SM, service threshold, and for
-// frames with network proposals the gate (1000: off), count and cell level.
+// A tuning setting: warp tile, blocks per SM, service threshold, for frames
+// with network proposals the gate (1000: off), count and cell level, and for
+// fused frames with two trees whether they split.
 struct TuneSetting {
   int shift, blocks, service;
   int gate, count, level;
+  int split;
 };
 
 TuneSetting current_setting(const qbc_ctx* c) {
-  return {c->tile_shift, c->blocks_per_sm, c->service_min, c->proposal_gate, c->proposal_count, c->proposal_level};
+  return {c->tile_shift, c->blocks_per_sm, c->service_min, c->proposal_gate, c->proposal_count, c->proposal_level,
+          c->split_trees};
 }
 
 void apply_setting(qbc_ctx* c, const TuneSetting& s) {
@@ -283,6 +289,7 @@ void apply_setting(qbc_ctx* c, const TuneSetting& s) {
   c->proposal_gate = s.gate;
   c->proposal_count = s.count;
   c->proposal_level = s.level;
+  c->split_trees = s.split;
 }
 
 // Median device time of `reps` frames (after one untimed frame).
@@ -323,38 +330,35 @@ int autotune_impl(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs, in
     }
     return QBC_OK;
   };
+  // each option swept with the others at their best so far
+  auto vary = [&](int TuneSetting::*f, std::initializer_list<int> vals) -> int {
+    for (int v : vals) {
+      if (v == best->*f) continue;
+      TuneSetting s = *best;
+      s.*f = v;
+      const int e = consider(s);
+      if (e) return e;
+    }
+    return QBC_OK;
+  };
   // network proposals first: whether they pay at all (gate 1000 is off),
   // how confident the network must be, how many to try, at which level
   if (opts && opts->proposals == QBC_PROPOSE_MLP) {
-    for (int g : {1000, 900, 700, 500, 300, 0})
-      if (g != best->gate && (rc = consider({best->shift, best->blocks, best->service, g, best->count, best->level})))
-        return rc;
+    if ((rc = vary(&TuneSetting::gate, {1000, 900, 700, 500, 300, 0}))) return rc;
     if (best->gate < 1000) {
-      for (int k : {1, 2, 3})
-        if (k != best->count &&
-            (rc = consider({best->shift, best->blocks, best->service, best->gate, k, best->level})))
-          return rc;
-      if (opts->proposal_level == 0)
-        for (int l : {5, 6, 7, 8})
-          if (l != best->level &&
-              (rc = consider({best->shift, best->blocks, best->service, best->gate, best->count, l})))
-            return rc;
+      if ((rc = vary(&TuneSetting::count, {1, 2, 3}))) return rc;
+      if (opts->proposal_level == 0 && (rc = vary(&TuneSetting::level, {5, 6, 7, 8}))) return rc;
     }
   }
-  // then the schedule, one option at a time, each kept at its best before
-  // the next is swept
-  for (int sm : {1, 2, 3, 4, 6, 8, 12, 16})
-    if (sm != best->service &&
-        (rc = consider({best->shift, best->blocks, sm, best->gate, best->count, best->level})))
-      return rc;
-  for (int sh : {1, 2, 3, 4, 5})
-    if (sh != best->shift &&
-        (rc = consider({sh, best->blocks, best->service, best->gate, best->count, best->level})))
-      return rc;
-  for (int bl : {0, 2, 3, 4, 6, 8})
-    if (bl != best->blocks &&
-        (rc = consider({best->shift, bl, best->service, best->gate, best->count, best->level})))
-      return rc;
+  // then the schedule, one option at a time
+  if ((rc = vary(&TuneSetting::service, {1, 2, 3, 4, 6, 8, 12, 16}))) return rc;
+  if ((rc = vary(&TuneSetting::shift, {1, 2, 3, 4, 5}))) return rc;
+  if ((rc = vary(&TuneSetting::blocks, {0, 2, 3, 4, 6, 8}))) return rc;
+  // a fused frame with two trees: one launch or the split, at the schedule
+  // found (its second launch's tail weighs differently per schedule)
+  if ((!opts || !opts->two_pass) && c->persistent && c->tree[1].n > 0 &&
+      (rc = vary(&TuneSetting::split, {0, 1})))
+    return rc;
   res->ms_best = best_ms;
   return QBC_OK;
 }
@@ -390,5 +394,6 @@ extern "C" int qbc_autotune(qbc_ctx* c, const qbc_view* views, const qbc_outputs
   result->proposal_gate = keep.gate;
   result->proposal_count = keep.count;
   result->proposal_level = keep.level;
+  result->split_trees = keep.split;
   return QBC_OK;
 }

@@ -80,6 +80,7 @@ struct qbc_ctx {
   int proposal_level = 8;   // level of the proposed cells when a render's options leave it 0
   int box_prune = 1;        // skip subtrees whose leaf boxes the ray misses
   int persistent = 1;       // fused frames on the persistent kernel (0: one thread per pixel)
+  int split_trees = 0;      // two-tree fused frames as a one-tree and a two-tree launch
   int64_t launches = 0;
   qbc::BuildScratch build;       // GPU tree build scratch, kept for per-frame rebuilds
   void* build_input = nullptr;   // device copy of host build input

@@ -26,6 +26,7 @@ enum DeviceError : unsigned {
   kErrBuildOctet = 2u,  // an octet path entry was outside 0..7
   kErrSkinBone = 4u,    // a skinned point named a bone outside the bone set
   kErrMmaTimeout = 8u,  // a bounded wait for the tensor cores gave up (the kernel stopped early)
+  kErrRecordOverflow = 16u,  // a split frame's record queue was full (pixels left unwritten)
 };
 
 // Scratch of the GPU tree build, owned by the context and reused by every

@@ -164,6 +164,11 @@ extern "C" int qbc_set_option(qbc_ctx* c, int option, int value) {
     c->persistent = value;
     return QBC_OK;
   }
+  if (option == QBC_OPT_SPLIT_TREES) {
+    if (value < 0 || value > 1) return fail(QBC_E_ARG, "qbc_set_option: split trees %d (0 or 1)", value);
+    c->split_trees = value;
+    return QBC_OK;
+  }
   return fail(QBC_E_ARG, "qbc_set_option: unknown option %d", option);
 }
 
@@ -201,6 +206,10 @@ extern "C" int qbc_get_option(qbc_ctx* c, int option, int* value) {
     *value = c->persistent;
     return QBC_OK;
   }
+  if (option == QBC_OPT_SPLIT_TREES) {
+    *value = c->split_trees;
+    return QBC_OK;
+  }
   return fail(QBC_E_ARG, "qbc_get_option: unknown option %d", option);
 }
 
@@ -211,6 +220,8 @@ int check_device_errors(qbc_ctx* c) {
   if (!h) return QBC_OK;
   QBC_CUDA(cudaMemsetAsync(c->derr, 0, sizeof(unsigned), c->stream));
   QBC_CUDA(cudaStreamSynchronize(c->stream));
+  if (h & qbc::kErrRecordOverflow)
+    return fail(QBC_E_STATE, "render: the record queue of a split frame was full; some pixels were not written");
   if (h & qbc::kErrMmaTimeout)
     return fail(QBC_E_TIMEOUT, "proposal network: a tensor-core wait gave up; the proposals of that render are incomplete");
   if (h & qbc::kErrSkinBone) return fail(QBC_E_ARG, "qbc_skin_rigid: a bone index was outside the bone set (point skinned with bone 0)");
@@ -832,7 +843,7 @@ int read_stats(qbc_ctx* c, qbc_render_stats* stats, bool two) {
   QBC_CUDA(cudaMemcpyAsync(h, c->wstats, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
   if (two) QBC_CUDA(cudaMemcpyAsync(q, c->wcount, sizeof(q), cudaMemcpyDeviceToHost, c->stream));
   QBC_CUDA(cudaStreamSynchronize(c->stream));
-  stats->queued = q[0];
+  stats->queued = two ? q[0] : h[qbc::kStatSplitQueued];
   stats->shadow_rays = h[qbc::kStatShadowRays];
   stats->shadow_visits = h[qbc::kStatShadowVisits];
   stats->proposals_tried = h[qbc::kStatPropTried];
@@ -857,9 +868,12 @@ int launch_render(qbc_ctx* c, const qbc::Batch& b, size_t smem, const qbc::Wave&
   if (c->blocks_per_sm > 0) per_sm = std::min(per_sm, c->blocks_per_sm);
   // persistent: one wave of resident blocks, never more blocks than warp tiles
   int64_t blocks = (int64_t)per_sm * c->sm_count;
-  if (MODE != qbc::kShadePass) blocks = std::min<int64_t>(blocks, ((int64_t)b.tiles_total + 3) / 4);
+  // (the split frame's two-tree kernel takes records, then the tiles its
+  // one-tree kernel left: the tile counter carries over)
+  constexpr bool tiles_only = MODE == qbc::kFused || MODE == qbc::kPrimaryPass || MODE == qbc::kSplitStatic;
+  if (tiles_only) blocks = std::min<int64_t>(blocks, ((int64_t)b.tiles_total + 3) / 4);
   blocks = std::max<int64_t>(blocks, 1);
-  if (MODE != qbc::kShadePass) QBC_CUDA(cudaMemsetAsync(c->queue, 0, sizeof(unsigned int), c->stream));
+  if (tiles_only) QBC_CUDA(cudaMemsetAsync(c->queue, 0, sizeof(unsigned int), c->stream));
   qbc::DevScene sc = device_scene(c);
   for (int i = 0; i < b.n; ++i)
     if (b.job[i].o.visits) sc.box_words = c->wstats + qbc::kStatBoxWords;  // an instrumented render
@@ -888,9 +902,58 @@ int launch_simple(qbc_ctx* c, const qbc::Batch& b, size_t smem) {
   return QBC_OK;
 }
 
+// A fused two-tree frame in two launches: the one-tree kernel walks every ray
+// that provably leaves the dynamic tree alone and queues each pixel whose
+// next ray may not (with its state and the phase to resume at); the
+// two-tree kernel finishes the queued pixels, then the tiles the one-tree
+// kernel left. A pixel leaves the one-tree kernel at most once. The queue
+// holds a quarter of the batch's pixels; once it may not hold every pixel
+// in flight (at most 64 per warp after a warp's last look at the count: the
+// 32 in its lanes and a new tile's 32), the one-tree kernel takes no new
+// tile.
+template <bool EXACT, bool DYN>
+int launch_split(qbc_ctx* c, const qbc::Batch& b, size_t smem, int64_t pixels) {
+  if constexpr (EXACT && DYN) {
+    const int64_t reserve = (int64_t)64 * 4 * 32 * c->sm_count;  // 64 per warp, 32 blocks of 4 warps per SM at most
+    const int64_t want = std::min<int64_t>(std::max<int64_t>(pixels / 4, 2 * reserve), pixels + reserve);
+    if (c->rec_cap < want) {
+      int rc = grow(&c->rec, &c->rec_cap, want, (size_t)qbc::kRecWords * 4, "render records");
+      if (rc) return rc;
+    }
+    qbc::Wave w{};
+    w.rec = c->rec;
+    w.qcount = c->wcount;
+    w.qnext = c->wcount + 1;
+    w.stats = c->wstats;
+    w.cap = (uint32_t)std::min<int64_t>(c->rec_cap, 0xFFFFFFFFll);
+    w.stop = (c->rec_cap >= pixels && pixels <= 0xFFFFFFFFll) ? 0xFFFFFFFFu : (uint32_t)(w.cap - reserve);
+    w.err = c->derr;
+    QBC_CUDA(cudaMemsetAsync(c->wcount, 0, 2 * sizeof(unsigned int), c->stream));
+    // the one-tree walk keeps 2 stack words per level, not 3
+    const size_t smem1 = smem - (size_t)b.max_level * qbc::kThreads * sizeof(uint32_t);
+    int rc = launch_render<true, false, qbc::kSplitStatic, false>(c, b, smem1, w);
+    if (rc) return rc;
+    return launch_render<true, true, qbc::kSplitFinish, false>(c, b, smem, w);
+  } else {
+    (void)b;
+    (void)smem;
+    (void)pixels;
+    return fail(QBC_E_STATE, "split frame: needs exact cubes and two trees");
+  }
+}
+
+// Whether a fused frame runs split: two trees, exact cubes, the dynamic
+// tree's leaf boxes built below its root and reached by the batch's depth.
+bool split_frame(const qbc_ctx* c, const qbc::Batch& b, bool exact, bool dyn) {
+  if (!exact || !dyn || !c->persistent || !c->split_trees) return false;
+  const qbc::DevTree t = device_scene(c).tree[1];
+  return t.cbox != nullptr && t.box_depth > 1 && b.max_level >= t.box_depth;
+}
+
 template <bool EXACT, bool DYN>
 int launch_modes(qbc_ctx* c, const qbc::Batch& b, size_t smem, const qbc_render_opts* opts, int64_t pixels) {
   if ((!opts || !opts->two_pass) && !c->persistent) return launch_simple<EXACT, DYN>(c, b, smem);
+  if ((!opts || !opts->two_pass) && split_frame(c, b, EXACT, DYN)) return launch_split<EXACT, DYN>(c, b, smem, pixels);
   if (!opts || !opts->two_pass) return launch_render<EXACT, DYN, qbc::kFused, false>(c, b, smem, qbc::Wave{});
   // two passes: primary rays -> record queue -> shade pass
   if (c->rec_cap < pixels) {

@@ -10,6 +10,7 @@
 // slowest ray of the warp.
 #pragma once
 
+#include "qbc_internal.h"
 #include "qbcuda.h"
 #include "walker.cuh"
 
@@ -120,9 +121,14 @@ constexpr int kRecWords = 32;
 constexpr int kRecProp = kPxProp;      // 3 floats: proposals (written between the passes)
 constexpr int kRecLogT = kPxProp + 3;  // float: t of the plain shadow walk's first leaf, -1 if none
 constexpr int kRecLogLit = kRecLogT + 1;  // lit bit of the plain shadow walk
+// Records of a split frame (kSplitStatic -> kSplitFinish): the phase whose
+// ray the pixel resumes with in the two-tree kernel (kPrimary, kShadow or
+// kFlare).
+constexpr int kRecResume = kRecLogLit + 1;
+static_assert(kRecResume < kRecWords, "record words");
 
 enum Phase : int { kIdle = 0, kPrimary = 1, kShadow = 2, kFlare = 3, kProposal = 4 };
-enum Mode : int { kFused = 0, kPrimaryPass = 1, kShadePass = 2 };
+enum Mode : int { kFused = 0, kPrimaryPass = 1, kShadePass = 2, kSplitStatic = 3, kSplitFinish = 4 };
 
 // Statistics of a render (uint64 each): the shade pass's counters, and the
 // leaf-box words read by the walks of an instrumented render.
@@ -133,6 +139,7 @@ enum Stat : int {
   kStatPropProven,       // shadow rays settled by a proposal
   kStatPropVisits,       // node visits of proposal walks
   kStatBoxWords,         // leaf-box words read (renders with a visits output)
+  kStatSplitQueued,      // pixels a split frame's one-tree kernel handed on
   kStatCount = 8
 };
 
@@ -146,6 +153,8 @@ struct Wave {
   int32_t nprop;                // proposals per record to try (0..3)
   int32_t pdepth;               // level of the proposed cells
   float* pixlog;                // per pixel of the batch: logged first-leaf t (-1 none), when log
+  uint32_t stop;                // kSplitStatic: no new tile once qcount exceeds this
+  unsigned* err;                // DeviceError bits (a split frame's record overflow)
 };
 
 // Internal flag: the pixel's camera ray is within the flare angle. The public
@@ -157,6 +166,13 @@ struct PixRef {
   __device__ __forceinline__ uint32_t& w(int k) const { return base[k * kThreads]; }
   __device__ __forceinline__ float& f(int k) const { return reinterpret_cast<float&>(base[k * kThreads]); }
 };
+
+// Lanes below this one in the warp (a special register: nothing held).
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
 
 // Octets of a point down to `depth` levels (octree.c:100-109), root first.
 __device__ __forceinline__ uint32_t point_path(float3 q, float basesize, int depth) {
@@ -172,6 +188,33 @@ __device__ __forceinline__ uint32_t point_path(float3 q, float basesize, int dep
     k = (k << 3) | (uint32_t)octet;
   }
   return k;
+}
+
+// kSplitStatic: the lanes whose new ray is not walked (defer) hand their
+// pixel, its state words px (stride kThreads) and the phase to resume at, to
+// the two-tree kernel: one atomic per warp. Out of line: it runs once per
+// handed-on ray, away from the walk's hot code.
+static __device__ __noinline__ void hand_on(bool defer, int phase, uint32_t* px, const Wave& wave) {
+  const unsigned dm = __ballot_sync(0xFFFFFFFFu, defer);
+  const int lead = __ffs((int)dm) - 1;
+  unsigned base = 0;
+  if ((int)(threadIdx.x & 31u) == lead) base = atomicAdd(wave.qcount, (unsigned)__popc(dm));
+  base = __shfl_sync(0xFFFFFFFFu, base, lead);
+  if (!defer) return;
+  const unsigned q = base + __popc(dm & lanemask_lt());
+  if (q >= wave.cap) {
+    atomicOr(wave.err, kErrRecordOverflow);  // wave.stop leaves room for every pixel in flight
+    return;
+  }
+  uint32_t* r = wave.rec + (size_t)q * kRecWords;
+  if (phase == kPrimary) {
+    r[kPxView] = px[kPxView * kThreads];
+    r[kPxXY] = px[kPxXY * kThreads];
+  } else {
+#pragma unroll
+    for (int k = 0; k < kRecCopy; ++k) r[k] = px[k * kThreads];
+  }
+  r[kRecResume] = (uint32_t)phase;
 }
 
 template <bool EXACT, bool DYN, int MODE, bool PROP>
@@ -284,11 +327,34 @@ struct Shader {
   // Shade pass: pixel of record q; sets its first ray into (rp, rd).
   __device__ __forceinline__ void begin_record(uint32_t q, float3& rp, float3& rd) {
     const uint32_t* r = wave.rec + (size_t)q * kRecWords;
+    rec_q = q;
+    if (MODE == kSplitFinish) {
+      // a split frame: the pixel resumes where the single-tree kernel left it
+      const int ph = (int)r[kRecResume];
+      if (ph == kPrimary) {
+        const uint32_t xy = r[kPxXY];
+        begin_pixel((int)r[kPxView], (int)(xy & 0xFFFFu), (int)(xy >> 16), rp, rd);
+        return;
+      }
+#pragma unroll
+      for (int k = 0; k < kRecCopy; ++k) px.w(k) = r[k];
+      const qbc_view& v = view();
+      maxlevel = v.maxlevel;
+      bc = held_bc<EXACT>(v);
+      prop_k = 0;
+      next_tdepth = 0;
+      if (ph == kShadow) {
+        shadow_ray(rp, rd);
+        phase = kShadow;
+      } else {
+        start_flare(rp, rd);
+      }
+      return;
+    }
 #pragma unroll
     for (int k = 0; k < kRecCopy; ++k) px.w(k) = r[k];
 #pragma unroll
     for (int k = 0; k < 3; ++k) px.w(kPxProp + k) = PROP ? r[kRecProp + k] : 0u;
-    rec_q = q;
     const qbc_view& v = view();
     maxlevel = v.maxlevel;
     bc = held_bc<EXACT>(v);
@@ -459,13 +525,6 @@ struct Shader {
   }
 };
 
-// Lanes below this one in the warp (a special register: nothing held).
-__device__ __forceinline__ unsigned lanemask_lt() {
-  unsigned m;
-  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-  return m;
-}
-
 // Global tile queue: 32-pixel warp tiles (8x4 by default), numbered view by
 // view.
 __device__ __forceinline__ int tile_view(const Batch& b, int tile) {
@@ -491,12 +550,22 @@ constexpr int kServiceMinDefault = 4;
 // record queue (warp-aggregated atomics), the rest are written.
 // MODE kShadePass: the queued pixels' shadow rays (first the proposals, with
 // PROP), shading and flare.
+// A fused frame with two trees may run split, as two launches:
+// MODE kSplitStatic (the one-tree kernel): as kFused, but a ray whose
+// two-tree walk would read the dynamic tree (Walker::walks_dynamic) is not
+// walked: its pixel goes with its state to the record queue. The other
+// rays' two-tree walks read the static tree alone, so the one-tree walk
+// gives them the same results with the lighter kernel. Once the queue may
+// not hold every pixel the warps can still hand on (wave.stop), no warp
+// takes a new tile.
+// MODE kSplitFinish (the two-tree kernel): the queued pixels, each from the
+// ray it stopped at, then the tiles the one-tree kernel left.
 // Minimum resident blocks per SM the register allocation must allow: the
 // walk is latency-bound per warp, so more resident warps pay as long as
-// nothing (or next to nothing) spills: 6 (80 registers) for the fused and
-// primary-pass kernels; the shade passes, which also shade and test
-// proposals, and the two-tree walk of an inexact basecube (which keeps the
-// node blocks live) keep 5 with both trees and no bound with one.
+// nothing (or next to nothing) spills: 6 (80 registers) for the fused,
+// primary-pass and split kernels; the shade passes, which also shade and
+// test proposals, and the two-tree walk of an inexact basecube (which keeps
+// the node blocks live) keep 5 with both trees and no bound with one.
 template <bool EXACT, bool DYN, int MODE>
 constexpr int render_min_blocks() {
   return (MODE == kShadePass || (DYN && !EXACT)) ? (DYN ? 5 : 1) : 6;
@@ -508,6 +577,7 @@ __global__ void __launch_bounds__(kThreads, render_min_blocks<EXACT, DYN, MODE>(
   extern __shared__ uint32_t smem[];
   const int tid = threadIdx.x, lane = tid & 31;
   constexpr int kW = Walker<EXACT, DYN, PROP>::kWords;
+  constexpr bool kRecords = MODE == kShadePass || MODE == kSplitFinish;
   Shader<EXACT, DYN, MODE, PROP> S{sc, batch, wave, Stack{smem + tid, kThreads},
                                    PixRef{smem + kW * batch.max_level * kThreads + tid}};
   S.phase = kIdle;
@@ -525,7 +595,9 @@ __global__ void __launch_bounds__(kThreads, render_min_blocks<EXACT, DYN, MODE>(
   int chunk = 0, consumed = 32;  // warp-uniform
   bool fast = false;             // warp-uniform: see the service phase
   bool exhausted = false;
-  const unsigned total = MODE == kShadePass ? min(*wave.qcount, wave.cap) : (unsigned)batch.tiles_total;
+  bool from_rec = kRecords;      // warp-uniform: the chunk is 32 records (else a tile)
+  const unsigned nrec = kRecords ? min(*wave.qcount, wave.cap) : 0u;
+  const unsigned ntiles = (unsigned)batch.tiles_total;
 
   for (;;) {
     const unsigned run = __ballot_sync(0xFFFFFFFFu, S.running);
@@ -557,11 +629,23 @@ __global__ void __launch_bounds__(kThreads, render_min_blocks<EXACT, DYN, MODE>(
       unsigned idle = __ballot_sync(0xFFFFFFFFu, S.phase == kIdle);
       while (idle && !exhausted) {
         if (consumed >= 32) {
-          unsigned t0 = 0;
-          if (lane == 0) t0 = atomicAdd(MODE == kShadePass ? wave.qnext : queue, MODE == kShadePass ? 32u : 1u);
+          unsigned t0 = 0, stop = 0;
+          if (lane == 0) {
+            if (MODE == kSplitStatic) stop = *(volatile unsigned*)wave.qcount > wave.stop ? 1u : 0u;
+            if (!stop) t0 = atomicAdd(from_rec ? wave.qnext : queue, from_rec ? 32u : 1u);
+          }
+          if (MODE == kSplitStatic && __shfl_sync(0xFFFFFFFFu, stop, 0)) {
+            exhausted = true;
+            break;
+          }
           chunk = (int)__shfl_sync(0xFFFFFFFFu, t0, 0);
           consumed = 0;
-          if ((unsigned)chunk >= total) {
+          if (MODE == kSplitFinish && from_rec && (unsigned)chunk >= nrec) {
+            from_rec = false;  // records done: the tiles left
+            consumed = 32;
+            continue;
+          }
+          if ((unsigned)chunk >= (from_rec ? nrec : ntiles)) {
             exhausted = true;
             break;
           }
@@ -570,9 +654,9 @@ __global__ void __launch_bounds__(kThreads, render_min_blocks<EXACT, DYN, MODE>(
         const int rank = __popc(idle & lanemask_lt());
         if (((idle >> lane) & 1u) && rank < avail) {
           const int slot = consumed + rank;
-          if (MODE == kShadePass) {
+          if (from_rec) {
             const unsigned q = (unsigned)chunk + slot;
-            if (q < total) {
+            if (q < nrec) {
               S.begin_record(q, rp, rd);
               go = true;
             }
@@ -592,9 +676,12 @@ __global__ void __launch_bounds__(kThreads, render_min_blocks<EXACT, DYN, MODE>(
         consumed += min(avail, __popc(idle));
         idle = __ballot_sync(0xFFFFFFFFu, S.phase == kIdle);
       }
+      bool defer = false;  // kSplitStatic: the new ray's two-tree walk would read the dynamic tree
       if (go) {
         if (S.w.start(S.bc, rp, rd, sc, S.maxlevel) == kDiscard) {
           S.discard();
+        } else if (MODE == kSplitStatic && S.w.walks_dynamic(sc, S.bc, S.maxlevel)) {
+          defer = true;
         } else {
           S.running = true;
           if (PROP && S.phase == kProposal) {
@@ -602,6 +689,10 @@ __global__ void __launch_bounds__(kThreads, render_min_blocks<EXACT, DYN, MODE>(
             S.w.tdepth = S.next_tdepth;
           }
         }
+      }
+      if (MODE == kSplitStatic && __any_sync(0xFFFFFFFFu, defer)) {
+        hand_on(defer, S.phase, S.px.base, wave);
+        if (defer) S.phase = kIdle;
       }
       // whether every running lane may divide by its reciprocals (the set
       // of running rays changes only here)
@@ -616,6 +707,7 @@ __global__ void __launch_bounds__(kThreads, render_min_blocks<EXACT, DYN, MODE>(
       }
     }
   }
+  if (MODE == kSplitFinish && blockIdx.x == 0 && tid == 0) atomicAdd(wave.stats + kStatSplitQueued, nrec);
   if (MODE == kShadePass) {
     // statistics: one atomic per warp and counter
 #pragma unroll

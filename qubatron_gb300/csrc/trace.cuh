@@ -346,4 +346,40 @@ __device__ __forceinline__ bool child_box_hit(uint2 r, int o, const BoxFrame& f)
   return (xlo < xhi) & (tn <= tf) & (tf >= 0.0f);  // xlo >= xhi + 1: a subtree without leaves
 }
 
+// Whether a ray may reach a leaf of tree t: false when every child of the
+// root is empty or its leaf box (widened by 2^-14 of the basecube edge) is
+// missed, the filter's own test at the root. The caller has established the
+// filter's conditions for the ray (exact basecube, nonzero direction
+// components, origin within 8 edges, boxes built for the render's depth);
+// without a usable box one level below the root the answer is true.
+__device__ __forceinline__ bool root_box_near(const DevTree& t, float4 bc, float3 p, float3 inv) {
+  if (t.cbox == nullptr || t.box_depth <= 1 || t.n == 0) return true;
+  const int4 r0 = __ldg(t.child), r1 = __ldg(t.child + 1);
+  uint32_t occ = 0;
+#pragma unroll
+  for (int o = 0; o < 8; ++o) occ |= pick8(r0, r1, o) > 0 ? (1u << o) : 0u;
+  if (occ == 0u) return false;
+  const BoxFrame bf = box_frame(bc, p, inv, bc.w * 6.1035156e-05f);
+  // occupied children only (a character fills one or two octants)
+#pragma unroll 1
+  for (; occ; occ &= occ - 1u) {
+    const int o = __ffs((int)occ) - 1;
+    if (child_box_hit(child_box_word(t.cbox, o), o, bf)) return true;
+  }
+  return false;
+}
+
+// The same test out of line (for a kernel that runs it once per ray start,
+// away from its walk's hot code); the tree's fields by value.
+static __device__ __noinline__ bool root_box_near_call(const int4* child, const uint32_t* cbox, int32_t box_depth,
+                                                       int32_t n, float4 bc, float3 p, float3 inv) {
+  DevTree t;
+  t.child = child;
+  t.cbox = cbox;
+  t.box_depth = box_depth;
+  t.n = n;
+  t.model = nullptr;
+  return root_box_near(t, bc, p, inv);
+}
+
 }  // namespace qbc

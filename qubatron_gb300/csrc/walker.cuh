@@ -31,6 +31,16 @@ namespace qbc {
 
 enum : int { kRunning = 3 };
 
+// Whether the leaf-box filter applies to an EXACT ray (fdiv: its plane hits
+// divide by reciprocals): every direction component nonzero (finite
+// reciprocals) and the origin within 8 basecube edges s (candidate points
+// then stay within ~2^-17 s of the ray, far inside the 2^-14 s margin).
+__device__ __forceinline__ bool box_ray_ok(float3 p, float3 d, float s, bool fdiv) {
+  const float r8 = 8.0f * s;
+  return fdiv & (d.x != 0.0f) & (d.y != 0.0f) & (d.z != 0.0f) & (fabsf(p.x) <= r8) & (fabsf(p.y) <= r8) &
+         (fabsf(p.z) <= r8);
+}
+
 template <bool EXACT, bool DYN, bool PROP = false>
 struct Walker {
   float3 p, d;   // ray origin and direction
@@ -112,24 +122,33 @@ struct Walker {
     tdepth = 0;
     if (EXACT) {
       const bool fdiv = recip_div_ok(p, d, bc.w);
-      // boxes: every direction component nonzero (finite reciprocals), the
-      // origin within 8 basecube edges (candidate points then stay within
-      // ~2^-17 S of the ray, far inside the 2^-14 S margin), and boxes built
-      // for a depth the render reaches
-      const float r8 = 8.0f * bc.w;
-      const bool geo = fdiv & (d.x != 0.0f) & (d.y != 0.0f) & (d.z != 0.0f) & (fabsf(p.x) <= r8) &
-                       (fabsf(p.y) <= r8) & (fabsf(p.z) <= r8);
+      // boxes: a ray the filter applies to, and boxes built for a depth the
+      // render reaches
+      const bool geo = box_ray_ok(p, d, bc.w, fdiv);
       const bool bs = geo & (sc.tree[0].cbox != nullptr) & (maxlevel >= sc.tree[0].box_depth);
       const bool bd = DYN & geo & (sc.tree[1].cbox != nullptr) & (maxlevel >= sc.tree[1].box_depth);
       mode = (fdiv ? 1u : 0u) | (bs ? 2u : 0u) | (bd ? 4u : 0u);
       inv = make_float3(d.x == 0.0f ? 0.0f : __frcp_rn(d.x), d.y == 0.0f ? 0.0f : __frcp_rn(d.y),
                         d.z == 0.0f ? 0.0f : __frcp_rn(d.z));
+      // bit 3: the ray misses the leaf box of every child of the dynamic
+      // root, so it can reach no dynamic leaf and the walk leaves the
+      // dynamic tree alone (the same pixels; no dynamic visits)
+      if (DYN && bd && !root_box_near(sc.tree[1], bc, p, inv)) mode |= 8u;
     }
     float4 h0;
     if (!entry(bc, h0)) return kDiscard;
     if (!EXACT) e0 = h0;
     e = h0;
     return kRunning;
+  }
+
+  // After start(): whether a two-tree walk of this ray reads the dynamic
+  // tree, i.e. Walker<EXACT, true>::start would not give it mode bit 3.
+  __device__ __forceinline__ bool walks_dynamic(const DevScene& sc, float4 bc, int maxlevel) const {
+    if (!EXACT) return true;
+    const DevTree& t = sc.tree[1];
+    if (!box_ray_ok(p, d, bc.w, (mode & 1u) != 0u) || t.cbox == nullptr || maxlevel < t.box_depth) return true;
+    return root_box_near_call(t.child, t.cbox, t.box_depth, t.n, bc, p, inv);
   }
 
   // Cube and entry point of level lv replayed from the root along the path.
@@ -161,11 +180,13 @@ struct Walker {
     if (EXACT) cube = cube_of_path(bc);
 
     // ---- subnode test (octree_fsh.c:251-329) ----
-    int4 s0, s1, d0, d1;
+    // dl: the ray walks the dynamic tree too (mode bit 3, set at the start)
+    const bool dl = DYN && (!EXACT || !(mode & 8u));
+    int4 s0, s1, d0 = make_int4(0, 0, 0, 0), d1 = d0;
     // with one tree a node below the root is always a child index > 0 (the
     // walk only enters occupied children), so the node-0 rule needs no test
     if (load_block(sc.tree[0], ns, DYN ? level : 0, s0, s1, oob)) ++vis_s;
-    if (DYN) {
+    if (dl) {
       if (load_block(sc.tree[1], nd, level, d0, d1, oob)) ++vis_d;
     }
     float4 cb = brb_of(cube);
@@ -403,7 +424,7 @@ struct Walker {
         cs = __ldg(reinterpret_cast<const int32_t*>(sc.tree[0].child) + 8 * (uint32_t)parent + (cc & 7));
       slot(st, level, 1) = (uint32_t)parent;
       if (DYN) {
-        cd = load_child(sc.tree[1], parent_d, level, cc & 7, oob);
+        cd = dl ? load_child(sc.tree[1], parent_d, level, cc & 7, oob) : 0;
         slot(st, level, 2) = (uint32_t)parent_d;
       }
     } else if (len > 0) {
@@ -493,5 +514,6 @@ struct Walker {
     if (DYN && md > 0) load_attr(sc.model[1], md, col, nrm, oob);
   }
 };
+
 
 }  // namespace qbc

@@ -205,6 +205,12 @@ def test_pruned_walk_matches_the_oracle_with_boxes(ctx, oracle, floor50k_scene):
     ref = [oracle.render(sc, oracle.QboView.from_bytes(v.to_bytes())) for v in views]
     for v, r in zip(views, ref):
         compare_frame(gpu_frame(ctx, v), r, "two trees", visits=True)
+    # the same frame split: a one-tree and a two-tree launch
+    ctx.set_option(L.OPT_SPLIT_TREES, 1)
+    for v, r in zip(views, ref):
+        compare_frame(gpu_frame(ctx, v), r, "two trees, split", visits=True)
+    ctx.set_option(L.OPT_SPLIT_TREES, 0)
+    _ray_parity(ctx, oracle, sc, pos, dirs, visits=True)
     got, _ = ctx.render_host_ex(views, STREAMS, two_pass=True)
     for g, r in zip(got, ref):
         compare_frame(g.arrays, r, "two trees, two-pass", visits=True)
