@@ -27,16 +27,21 @@ using bf16 = __nv_bfloat16;
 // Network input of a shade-pass record: hit point normalised to the
 // basecube, unit normal, unit direction to the light, and sin/cos of pi
 // times the normalised hit point scaled by 4, 8, ..., 128 (45 values, zero
-// padded).
-__device__ __forceinline__ void record_features(const qbc::Batch& b, const uint32_t* r, bf16* x) {
-  const qbc_view& v = b.job[r[qbc::kPxView]].v;
+// padded). The normal is the primary leaf's, fetched again as the render
+// fetched it.
+__device__ __forceinline__ void record_features(const qbc::DevScene& sc, const qbc::Batch& b, const uint32_t* r,
+                                                bf16* x) {
+  const qbc_view& v = b.job[r[qbc::kRecView] & 0xFFu].v;
   const float S = v.basecube[3];
   const float lo[3] = {v.basecube[0], v.basecube[1] - S, v.basecube[2] - S};
+  float4 col = make_float4(0.0f, 0.0f, 0.0f, 0.0f), nrm = col;
+  if (r[qbc::kRecFlags] & QBC_PX_PRIMARY_LEAF)
+    qbc::leaf_texel(sc, sc.tree[1].n > 0, (int32_t)r[qbc::kRecLeaf], (int32_t)r[qbc::kRecLeaf + 1], v.maxlevel, col,
+                    nrm);
   float f[qbc::mlp::kIn];
-  float isp[3], n[3], l[3];
+  float isp[3], n[3] = {nrm.x, nrm.y, nrm.z}, l[3];
   for (int k = 0; k < 3; ++k) {
-    isp[k] = __uint_as_float(r[qbc::kPxIsp + k]);
-    n[k] = __uint_as_float(r[qbc::kPxNrm + k]);
+    isp[k] = __uint_as_float(r[qbc::kRecIsp + k]);
     l[k] = v.light[k] - isp[k];
   }
   const float nn = rsqrtf(fmaxf(n[0] * n[0] + n[1] * n[1] + n[2] * n[2], 1e-20f));
@@ -59,20 +64,21 @@ __device__ __forceinline__ void record_features(const qbc::Batch& b, const uint3
 }
 
 // Shaded records of a logged render -> training samples (appended).
-__global__ void collect_kernel(const __grid_constant__ qbc::Batch b, const __grid_constant__ qbc::Wave w,
+__global__ void collect_kernel(const qbc::DevScene sc, const __grid_constant__ qbc::Batch b,
+                               const __grid_constant__ qbc::Wave w,
                                bf16* __restrict__ X, float* __restrict__ tl, int8_t* __restrict__ kind,
                                unsigned int* __restrict__ count, int64_t cap) {
   const unsigned total = min(*w.qcount, w.cap);
   for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
     const uint32_t* r = w.rec + (size_t)q * qbc::kRecWords;
-    if (!(r[qbc::kPxFlags] & QBC_PX_SHADED)) continue;
+    if (!(r[qbc::kRecFlags] & QBC_PX_SHADED)) continue;
     const float t = __uint_as_float(r[qbc::kRecLogT]);
     const bool lit = r[qbc::kRecLogLit] != 0;
     const bool occluded = !lit && t > 0.0f && t < 1.0f;
     if (!lit && !occluded) continue;  // unlit without an occluder before the hit: no label
     const unsigned i = atomicAdd(count, 1u);
     if ((int64_t)i >= cap) continue;
-    record_features(b, r, X + (size_t)i * qbc::mlp::kIn);
+    record_features(sc, b, r, X + (size_t)i * qbc::mlp::kIn);
     tl[i] = occluded ? t : 2.0f;
     kind[i] = occluded ? 1 : 0;
   }
@@ -82,6 +88,7 @@ __global__ void collect_kernel(const __grid_constant__ qbc::Batch b, const __gri
 // record in, its proposals out (earliest first; none where the occlusion
 // logit is below the gate). The row count is read on the device.
 struct RecordRows {
+  qbc::DevScene sc;
   qbc::Batch b;
   qbc::Wave w;
   float gate;
@@ -91,7 +98,7 @@ struct RecordRows {
     if (lane >= 16) return;
     bf16* row = x + lane * qbc::mlp::kLdIn;
     if ((uint32_t)lane < n) {
-      record_features(b, w.rec + (size_t)(r0 + lane) * qbc::kRecWords, row);
+      record_features(sc, b, w.rec + (size_t)(r0 + lane) * qbc::kRecWords, row);
     } else {
       for (int k = 0; k < qbc::mlp::kIn; ++k) row[k] = __float2bfloat16(0.0f);
     }
@@ -230,6 +237,7 @@ int ensure_dataset(qbc_ctx* c, int64_t cap) {
 int propose_mlp(qbc_ctx* c, const qbc::Batch& b, const qbc::Wave& w) {
   if (!c->net.ready) return fail(QBC_E_STATE, "qbc_render_views_ex: no occluder network in this context");
   std::unique_ptr<RecordRows> src(new RecordRows());
+  src->sc = device_scene(c);
   src->b = b;
   src->w = w;
   const float p = (float)c->proposal_gate * 1e-3f;  // gate probability -> logit
@@ -296,8 +304,8 @@ extern "C" int qbc_proposal_collect(qbc_ctx* c, const qbc_view* views, int n, in
     w.rec = c->rec;
     w.qcount = c->wcount;
     w.cap = (uint32_t)std::min<int64_t>(c->rec_cap, 0xFFFFFFFFll);
-    collect_kernel<<<launch_grid(c, queued), 256, 0, c->stream>>>(*b, w, c->ds_x, c->ds_t, c->ds_kind,
-                                                                  c->ds_count, c->ds_cap);
+    collect_kernel<<<launch_grid(c, queued), 256, 0, c->stream>>>(device_scene(c), *b, w, c->ds_x, c->ds_t,
+                                                                  c->ds_kind, c->ds_count, c->ds_cap);
     delete b;
     QBC_CUDA(cudaGetLastError());
     ++c->launches;

@@ -782,8 +782,8 @@ __global__ void fill_logged_proposals(const __grid_constant__ Batch batch, const
   const unsigned total = min(*wave.qcount, wave.cap);
   for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
     uint32_t* r = wave.rec + (size_t)q * kRecWords;
-    const ViewJob& J = batch.job[r[kPxView]];
-    const uint32_t xy = r[kPxXY];
+    const ViewJob& J = batch.job[r[kRecView] & 0xFFu];
+    const uint32_t xy = r[kRecXY];
     const float t = wave.pixlog[J.pixel_begin + (int64_t)(xy >> 16) * J.v.width_px + (xy & 0xFFFFu)];
     reinterpret_cast<float&>(r[kRecProp]) = t;
     reinterpret_cast<float&>(r[kRecProp + 1]) = -1.0f;
@@ -795,7 +795,7 @@ __global__ void fill_random_proposals(const __grid_constant__ Wave wave, unsigne
   const unsigned total = min(*wave.qcount, wave.cap);
   for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
     uint32_t* r = wave.rec + (size_t)q * kRecWords;
-    unsigned long long z = seed + 0x9E3779B97F4A7C15ull * (r[kPxXY] + 0x10001ull * r[kPxView] + 1);
+    unsigned long long z = seed + 0x9E3779B97F4A7C15ull * (r[kRecXY] + 0x10001ull * (r[kRecView] & 0xFFu) + 1);
     for (int k = 0; k < 3; ++k) {
       z += 0x9E3779B97F4A7C15ull;
       unsigned long long x = z;
@@ -916,17 +916,20 @@ int launch_split(qbc_ctx* c, const qbc::Batch& b, size_t smem, int64_t pixels) {
   if constexpr (EXACT && DYN) {
     const int64_t reserve = (int64_t)64 * 4 * 32 * c->sm_count;  // 64 per warp, 32 blocks of 4 warps per SM at most
     const int64_t want = std::min<int64_t>(std::max<int64_t>(pixels / 4, 2 * reserve), pixels + reserve);
-    if (c->rec_cap < want) {
-      int rc = grow(&c->rec, &c->rec_cap, want, (size_t)qbc::kRecWords * 4, "render records");
+    // (the record buffer counts kRecWords units; a split record takes two)
+    constexpr int64_t kUnits = qbc::kSplitRecWords / qbc::kRecWords;
+    if (c->rec_cap < kUnits * want) {
+      int rc = grow(&c->rec, &c->rec_cap, kUnits * want, (size_t)qbc::kRecWords * 4, "render records");
       if (rc) return rc;
     }
+    const int64_t split_cap = c->rec_cap / kUnits;
     qbc::Wave w{};
     w.rec = c->rec;
     w.qcount = c->wcount;
     w.qnext = c->wcount + 1;
     w.stats = c->wstats;
-    w.cap = (uint32_t)std::min<int64_t>(c->rec_cap, 0xFFFFFFFFll);
-    w.stop = (c->rec_cap >= pixels && pixels <= 0xFFFFFFFFll) ? 0xFFFFFFFFu : (uint32_t)(w.cap - reserve);
+    w.cap = (uint32_t)std::min<int64_t>(split_cap, 0xFFFFFFFFll);
+    w.stop = (split_cap >= pixels && pixels <= 0xFFFFFFFFll) ? 0xFFFFFFFFu : (uint32_t)(w.cap - reserve);
     w.err = c->derr;
     QBC_CUDA(cudaMemsetAsync(c->wcount, 0, 2 * sizeof(unsigned int), c->stream));
     // the one-tree walk keeps 2 stack words per level, not 3

@@ -99,9 +99,7 @@ __device__ __forceinline__ float4 held_bc(const qbc_view& v) {
   return EXACT ? make_float4(0.0f, s, s, s) : view_bc(v);
 }
 
-// Per-lane pixel state in shared memory, word k at px[k * kThreads]. The
-// first kRecCopy words are also the record a primary pass hands to the
-// shade pass.
+// Per-lane pixel state in shared memory, word k at px[k * kThreads].
 enum PixWord : int {
   kPxView = 0, kPxXY, kPxFlags,
   kPxCsv,                  // 3 words: camera ray direction
@@ -113,19 +111,33 @@ enum PixWord : int {
   kPxProp = kPxVis + 4,    // 3 words: proposed shadow-ray t of the shade pass
   kPxEnd = kPxProp + 3
 };
-constexpr int kRecCopy = kPxProp;  // words a record carries from the primary pass
 static_assert(kPxEnd <= kPixWords, "pixel state");
 
-// Records of the two-pass render: 32 words per shaded or flare pixel.
-constexpr int kRecWords = 32;
-constexpr int kRecProp = kPxProp;      // 3 floats: proposals (written between the passes)
-constexpr int kRecLogT = kPxProp + 3;  // float: t of the plain shadow walk's first leaf, -1 if none
-constexpr int kRecLogLit = kRecLogT + 1;  // lit bit of the plain shadow walk
-// Records of a split frame (kSplitStatic -> kSplitFinish): the phase whose
-// ray the pixel resumes with in the two-tree kernel (kPrimary, kShadow or
-// kFlare).
-constexpr int kRecResume = kRecLogLit + 1;
-static_assert(kRecResume < kRecWords, "record words");
+// Records: 16 words per pixel one kernel hands to the next (the primary pass
+// to the shade pass of a two-pass render; a split frame's one-tree kernel
+// to its two-tree kernel). The camera ray, the primary texel and the normal
+// are not carried: the reader recomputes them from the view, the pixel and
+// the primary leaf, with the writer's own loads and arithmetic.
+enum RecWord : int {
+  kRecView = 0,              // view index (bits 0-7) | phase to resume at << 8 (split frames)
+  kRecXY, kRecFlags,
+  kRecIsp,                   // 4 words: primary intersection
+  kRecLeaf = kRecIsp + 4,    // 2 words: primary leaf s, d
+  kRecVis = kRecLeaf + 2,    // 2 words: primary visits s, d
+  kRecProp = kRecVis + 2,    // 3 floats: proposals (two-pass; written between the passes)
+  kRecShadow = kRecProp,     // split frames resuming at the flare ray: shadow leaf s, d, visits s, d
+  kRecLogT = kRecProp + 3,   // float: t of the plain shadow walk's first leaf, -1 if none
+  kRecLogLit,                // lit bit of the plain shadow walk
+  kRecWords,
+  // a split frame's records carry the state that a shade pass would
+  // recompute: its two-tree kernel then resumes a pixel with no reloads
+  // (its queue holds a quarter of the pixels, so they may be larger)
+  kRecCsv = kRecWords,       // 3 words: camera ray direction
+  kRecCol = kRecCsv + 3,     // 4 words: colour (primary texel, or shaded)
+  kRecNrm = kRecCol + 4,     // 3 words: primary normal
+  kSplitRecWords = 32
+};
+static_assert(kRecWords == 16 && kRecShadow + 4 <= kRecWords && kRecNrm + 3 <= kSplitRecWords, "record words");
 
 enum Phase : int { kIdle = 0, kPrimary = 1, kShadow = 2, kFlare = 3, kProposal = 4 };
 enum Mode : int { kFused = 0, kPrimaryPass = 1, kShadePass = 2, kSplitStatic = 3, kSplitFinish = 4 };
@@ -190,6 +202,53 @@ __device__ __forceinline__ uint32_t point_path(float3 q, float basesize, int dep
   return k;
 }
 
+// Record q of a pixel whose state words are px (stride kThreads), to resume
+// at `phase` (0: a two-pass record, for the shade pass; else a split
+// frame's, kSplitRecWords long). A pixel that resumes at its primary ray
+// needs only its view and position.
+__device__ __forceinline__ void write_record(uint32_t* r, const uint32_t* px, uint32_t phase) {
+  r[kRecView] = px[kPxView * kThreads] | (phase << 8);
+  r[kRecXY] = px[kPxXY * kThreads];
+  if (phase == kPrimary) return;
+  r[kRecFlags] = px[kPxFlags * kThreads];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) r[kRecIsp + k] = px[(kPxIsp + k) * kThreads];
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    r[kRecLeaf + k] = px[(kPxLeaf + k) * kThreads];
+    r[kRecVis + k] = px[(kPxVis + k) * kThreads];
+  }
+  if (phase == kFlare) {
+    // the shadow walk already ran: its leaf and visits
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      r[kRecShadow + k] = px[(kPxLeaf + 2 + k) * kThreads];
+      r[kRecShadow + 2 + k] = px[(kPxVis + 2 + k) * kThreads];
+    }
+  }
+  if (phase != 0u) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      r[kRecCsv + k] = px[(kPxCsv + k) * kThreads];
+      r[kRecNrm + k] = px[(kPxNrm + k) * kThreads];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) r[kRecCol + k] = px[(kPxCol + k) * kThreads];
+  }
+}
+
+// Texel and normal of the primary leaf (ns, nd) at `level`: the leaf fetch of
+// Walker::leaf (octree_fsh.c:218-247), the dynamic model winning where it
+// holds the leaf; dyn: the render walked a dynamic tree.
+__device__ __forceinline__ void leaf_texel(const DevScene& sc, bool dyn, int32_t ns, int32_t nd, int level,
+                                           float4& col, float4& nrm) {
+  bool oob = false;  // (the walk that found the leaf reported it)
+  const int32_t ms = load_model(sc.tree[0], ns, level, oob);
+  const int32_t md = dyn ? load_model(sc.tree[1], nd, level, oob) : 0;
+  load_attr(sc.model[0], ms, col, nrm, oob);
+  if (md > 0) load_attr(sc.model[1], md, col, nrm, oob);
+}
+
 // kSplitStatic: the lanes whose new ray is not walked (defer) hand their
 // pixel, its state words px (stride kThreads) and the phase to resume at, to
 // the two-tree kernel: one atomic per warp. Out of line: it runs once per
@@ -206,15 +265,7 @@ static __device__ __noinline__ void hand_on(bool defer, int phase, uint32_t* px,
     atomicOr(wave.err, kErrRecordOverflow);  // wave.stop leaves room for every pixel in flight
     return;
   }
-  uint32_t* r = wave.rec + (size_t)q * kRecWords;
-  if (phase == kPrimary) {
-    r[kPxView] = px[kPxView * kThreads];
-    r[kPxXY] = px[kPxXY * kThreads];
-  } else {
-#pragma unroll
-    for (int k = 0; k < kRecCopy; ++k) r[k] = px[k * kThreads];
-  }
-  r[kRecResume] = (uint32_t)phase;
+  write_record(wave.rec + (size_t)q * kSplitRecWords, px, (uint32_t)phase);
 }
 
 template <bool EXACT, bool DYN, int MODE, bool PROP>
@@ -324,25 +375,47 @@ struct Shader {
     return false;
   }
 
-  // Shade pass: pixel of record q; sets its first ray into (rp, rd).
+  // Shade pass: the pixel of record q; sets its first ray into (rp, rd). The
+  // camera ray, the primary texel and normal are recomputed, as begin_pixel
+  // and the primary leaf fetch made them. A split frame's two-tree kernel
+  // resumes the pixel from its record's state at the ray it stopped at.
   __device__ __forceinline__ void begin_record(uint32_t q, float3& rp, float3& rd) {
-    const uint32_t* r = wave.rec + (size_t)q * kRecWords;
+    constexpr int kStride = MODE == kSplitFinish ? kSplitRecWords : kRecWords;
+    const uint32_t* r = wave.rec + (size_t)q * kStride;
     rec_q = q;
-    if (MODE == kSplitFinish) {
-      // a split frame: the pixel resumes where the single-tree kernel left it
-      const int ph = (int)r[kRecResume];
-      if (ph == kPrimary) {
-        const uint32_t xy = r[kPxXY];
-        begin_pixel((int)r[kPxView], (int)(xy & 0xFFFFu), (int)(xy >> 16), rp, rd);
-        return;
-      }
-#pragma unroll
-      for (int k = 0; k < kRecCopy; ++k) px.w(k) = r[k];
+    const uint32_t vw = r[kRecView], xy = r[kRecXY];
+    const int ph = MODE == kSplitFinish ? (int)(vw >> 8) : 0;
+    if (MODE != kSplitFinish || ph == kPrimary) {
+      begin_pixel((int)(vw & 0xFFu), (int)(xy & 0xFFFFu), (int)(xy >> 16), rp, rd);
+      if (MODE == kSplitFinish) return;
+    } else {
+      px.w(kPxView) = vw & 0xFFu;
+      px.w(kPxXY) = xy;
       const qbc_view& v = view();
       maxlevel = v.maxlevel;
       bc = held_bc<EXACT>(v);
-      prop_k = 0;
-      next_tdepth = 0;
+    }
+    const uint32_t flags = r[kRecFlags];
+    px.w(kPxFlags) = flags;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) px.w(kPxIsp + k) = r[kRecIsp + k];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      px.w(kPxLeaf + k) = r[kRecLeaf + k];
+      px.w(kPxVis + k) = r[kRecVis + k];
+      px.w(kPxLeaf + 2 + k) = MODE == kSplitFinish && ph == kFlare ? r[kRecShadow + k] : (uint32_t)-1;
+      px.w(kPxVis + 2 + k) = MODE == kSplitFinish && ph == kFlare ? r[kRecShadow + 2 + k] : 0u;
+    }
+    prop_k = 0;
+    next_tdepth = 0;
+    if (MODE == kSplitFinish) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        px.w(kPxCsv + k) = r[kRecCsv + k];
+        px.w(kPxNrm + k) = r[kRecNrm + k];
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) px.w(kPxCol + k) = r[kRecCol + k];
       if (ph == kShadow) {
         shadow_ray(rp, rd);
         phase = kShadow;
@@ -351,16 +424,19 @@ struct Shader {
       }
       return;
     }
+    float4 col = make_float4(0.0f, 0.0f, 0.0f, 0.0f), nrm = col;
+    if (flags & QBC_PX_PRIMARY_LEAF)
+      leaf_texel(sc, DYN, (int32_t)r[kRecLeaf], (int32_t)r[kRecLeaf + 1], maxlevel, col, nrm);
 #pragma unroll
-    for (int k = 0; k < kRecCopy; ++k) px.w(k) = r[k];
+    for (int k = 0; k < 4; ++k) px.f(kPxCol + k) = (&col.x)[k];
+    if (flags & QBC_PX_SHADED) {
+      px.f(kPxNrm) = nrm.x;
+      px.f(kPxNrm + 1) = nrm.y;
+      px.f(kPxNrm + 2) = nrm.z;
+    }
 #pragma unroll
     for (int k = 0; k < 3; ++k) px.w(kPxProp + k) = PROP ? r[kRecProp + k] : 0u;
-    const qbc_view& v = view();
-    maxlevel = v.maxlevel;
-    bc = held_bc<EXACT>(v);
-    prop_k = 0;
-    next_tdepth = 0;
-    if (px.w(kPxFlags) & QBC_PX_SHADED) {
+    if (flags & QBC_PX_SHADED) {
       shadow_ray(rp, rd);
       phase = kShadow;
       if (PROP && next_proposal(rp, rd)) phase = kProposal;
@@ -616,11 +692,7 @@ __global__ void __launch_bounds__(kThreads, render_min_blocks<EXACT, DYN, MODE>(
           base = __shfl_sync(0xFFFFFFFFu, base, __ffs(enq) - 1);
           if (S.enqueue) {
             const unsigned q = base + __popc(enq & lanemask_lt());
-            if (q < wave.cap) {
-              uint32_t* r = wave.rec + (size_t)q * kRecWords;
-#pragma unroll
-              for (int k = 0; k < kRecCopy; ++k) r[k] = S.px.w(k);
-            }
+            if (q < wave.cap) write_record(wave.rec + (size_t)q * kRecWords, S.px.base, 0u);
             S.enqueue = false;
             S.phase = kIdle;
           }
