@@ -932,8 +932,7 @@ int launch_split(qbc_ctx* c, const qbc::Batch& b, size_t smem, int64_t pixels) {
     w.stop = (split_cap >= pixels && pixels <= 0xFFFFFFFFll) ? 0xFFFFFFFFu : (uint32_t)(w.cap - reserve);
     w.err = c->derr;
     QBC_CUDA(cudaMemsetAsync(c->wcount, 0, 2 * sizeof(unsigned int), c->stream));
-    // the one-tree walk keeps 2 stack words per level, not 3
-    const size_t smem1 = smem - (size_t)b.max_level * qbc::kThreads * sizeof(uint32_t);
+    const size_t smem1 = qbc::render_smem(b.max_level, false, false);
     int rc = launch_render<true, false, qbc::kSplitStatic, false>(c, b, smem1, w);
     if (rc) return rc;
     return launch_render<true, true, qbc::kSplitFinish, false>(c, b, smem, w);
@@ -1000,7 +999,7 @@ int launch_modes(qbc_ctx* c, const qbc::Batch& b, size_t smem, const qbc_render_
     rc = propose_mlp(c, b, w);
     if (rc) return rc;
   }
-  if (w.nprop > 0) rc = launch_render<EXACT, DYN, qbc::kShadePass, true>(c, b, smem, w);
+  if (w.nprop > 0) rc = launch_render<EXACT, DYN, qbc::kShadePass, true>(c, b, qbc::render_smem(b.max_level, DYN, true), w);
   else rc = launch_render<EXACT, DYN, qbc::kShadePass, false>(c, b, smem, w);
   if (rc) return rc;
   if (opts->log) c->pixlog_valid = pixels;
@@ -1033,8 +1032,7 @@ int launch_batch(qbc_ctx* c, const qbc_view* views, const qbc_outputs* dev_outs,
   b->service_min = c->service_min;
   b->tile_shift = c->tile_shift;
   const bool dyn = c->tree[1].n > 0;
-  const size_t words = (size_t)(dyn ? 3 : 2) * maxlevel + qbc::kPixWords;
-  const size_t smem = words * qbc::kThreads * sizeof(uint32_t);
+  const size_t smem = qbc::render_smem(maxlevel, dyn, false);
   int rc;
   if (exact)
     rc = dyn ? launch_modes<true, true>(c, *b, smem, opts, pixels) : launch_modes<true, false>(c, *b, smem, opts, pixels);
@@ -1433,7 +1431,7 @@ extern "C" int qbc_render_views_noalloc(qbc_ctx* c, const qbc_view* views, const
     b.max_level = maxlevel;
     b.service_min = c->service_min;
     b.tile_shift = c->tile_shift;
-    const size_t smem = ((size_t)(dyn ? 3 : 2) * maxlevel + qbc::kPixWords) * qbc::kThreads * sizeof(uint32_t);
+    const size_t smem = qbc::render_smem(maxlevel, dyn, false);
     unsigned int* q = queues + l;
     if (exact)
       rc = dyn ? launch_render_noalloc<true, true>(c, b, smem, q) : launch_render_noalloc<true, false>(c, b, smem, q);
