@@ -112,18 +112,18 @@ enum PixWord : int {
   kPxEnd = kPxProp + 3
 };
 static_assert(kPxEnd <= kPixWords, "pixel state");
-// Pixel state words the host allocates for a kernel: the two-tree kernels
-// that test no proposals leave the proposal words out. Each word is 512
-// bytes of a 128-thread block; without them six blocks of the two-tree
-// kernel fit a 196 KB shared-memory carveout instead of 228 KB, which
-// doubles its L1 cache (hit rate 33 % -> 63 %, -2 % time). The one-tree
-// kernels measured 0.6 % slower with the smaller block, so they keep all.
-__host__ __device__ constexpr int pix_words(bool dyn, bool prop) { return (dyn && !prop) ? kPxProp : kPxEnd; }
+// Pixel state words the host allocates for a kernel: the kernels that test
+// no proposals leave the proposal words out. Each word is 512 bytes of a
+// 128-thread block; without them six blocks of the two-tree kernel fit a
+// 196 KB shared-memory carveout instead of 228 KB, which doubles its L1
+// cache (hit rate 33 % -> 63 %, 2-3 % less time); the one-tree kernels
+// measured the same either way.
+__host__ __device__ constexpr int pix_words(bool prop) { return prop ? kPxEnd : kPxProp; }
 
 // Dynamic shared memory of a render kernel: its stack (2 words per level,
 // 3 with two trees) and its pixel state, per thread of a block.
 __host__ __device__ constexpr size_t render_smem(int max_level, bool dyn, bool prop) {
-  return ((size_t)(dyn ? 3 : 2) * (size_t)max_level + (size_t)pix_words(dyn, prop)) * kThreads * sizeof(uint32_t);
+  return ((size_t)(dyn ? 3 : 2) * (size_t)max_level + (size_t)pix_words(prop)) * kThreads * sizeof(uint32_t);
 }
 
 // Records: 16 words per pixel one kernel hands to the next (the primary pass
@@ -372,8 +372,8 @@ struct Shader {
 
   // The next usable proposal from prop_k on: the level-pdepth cell around
   // the proposed point of the shadow ray. Returns false when none is left.
-  // (Launches without PROP have wave.nprop 0: the proposal words, which the
-  // two-tree kernels without PROP do not keep, are never read.)
+  // (Launches without PROP have wave.nprop 0: the proposal words, which
+  // their kernels do not keep, are never read.)
   __device__ __forceinline__ bool next_proposal(float3 rp, float3 rd) {
     while (prop_k < wave.nprop) {
       const float t = px.f(kPxProp + prop_k);
