@@ -353,7 +353,9 @@ int autotune_impl(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs, in
   // then the schedule, one option at a time
   if ((rc = vary(&TuneSetting::service, {1, 2, 3, 4, 6, 8, 12, 16}))) return rc;
   if ((rc = vary(&TuneSetting::shift, {1, 2, 3, 4, 5}))) return rc;
-  if ((rc = vary(&TuneSetting::blocks, {0, 2, 3, 4, 6, 8}))) return rc;
+  // (5 blocks of a two-tree kernel fit a 164 KB shared-memory carveout:
+  // more L1 for fewer warps)
+  if ((rc = vary(&TuneSetting::blocks, {0, 2, 3, 4, 5, 6, 8}))) return rc;
   // a fused frame with two trees: one launch or the split, at the schedule
   // found (its second launch's tail weighs differently per schedule)
   if ((!opts || !opts->two_pass) && c->persistent && c->tree[1].n > 0 &&
