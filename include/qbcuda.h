@@ -289,7 +289,10 @@ int qbc_camera_rays(qbc_ctx* ctx, const qbc_view* view, const int32_t* px, const
  * pointers are rejected with QBC_E_ARG. Building leaf
  * boxes (QBC_OPT_BOX_PRUNE) allocates, so this call never builds them: it
  * prunes with the boxes an earlier allocating render built for the current
- * trees, and walks a tree changed since then unpruned (same pixels).
+ * trees, and walks a tree changed since then unpruned (same pixels). The
+ * frame always runs on the persistent fused kernel: QBC_OPT_PERSISTENT 0 and
+ * QBC_OPT_SPLIT_TREES 1 (whose record queue this call would have to
+ * allocate) do not apply to it.
  */
 #define QBC_NOALLOC_MAX_LAUNCHES 8
 #define QBC_NOALLOC_MAX_VIEWS (QBC_NOALLOC_MAX_LAUNCHES * 32)
