@@ -105,6 +105,12 @@ def test_pruned_two_tree_walk_keeps_every_pixel(oracle):
     for k in ("rgba", "rgba8", "flags", "leaf", "isp"):
         assert np.array_equal(a[k].view(np.uint8), b[k].view(np.uint8)), k
     assert b["visits"].sum() < a["visits"].sum()
+    assert (b["visits"] <= a["visits"]).all()
+    # the root rule: a primary ray that misses the leaf boxes of the dynamic
+    # root's children walks the static tree alone (no dynamic visits), though
+    # the shader's walk reads dynamic nodes on its way
+    skipped = (b["visits"][..., 1] == 0) & (a["visits"][..., 1] > 0)
+    assert skipped.sum() > 0
 
 
 def test_no_pruning_where_the_filter_does_not_apply(oracle):
