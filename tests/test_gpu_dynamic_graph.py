@@ -114,7 +114,7 @@ def test_dynamic_update_each_frame(env, oracle, floor50k_scene):
             compare_frame(g.arrays, ref, f"frame {frame}")
 
 
-@pytest.mark.parametrize("kind", ["fused", "two_pass_random"])
+@pytest.mark.parametrize("kind", ["fused", "fused_split", "two_pass_random"])
 def test_dynamic_graph_replays_equal_eager(env, floor50k_scene, kind):
     torch, ctx = env
     import qubatron_gb300 as qb
@@ -122,7 +122,10 @@ def test_dynamic_graph_replays_equal_eager(env, floor50k_scene, kind):
     upload_scene(ctx, s.nodes, s.colors, s.normals)
     rig = Rig(torch, ctx)
     views = _views()
-    kw = {} if kind == "fused" else {"two_pass": True, "proposals": qb._lib.PROPOSE_RANDOM, "seed": 7}
+    # fused_split: the frame as a one-tree and a two-tree launch (its record
+    # queue grown by the eager frame before the capture)
+    ctx.set_option(qb._lib.OPT_SPLIT_TREES, 1 if kind == "fused_split" else 0)
+    kw = {} if kind.startswith("fused") else {"two_pass": True, "proposals": qb._lib.PROPOSE_RANDOM, "seed": 7}
     gbufs, gouts = _outputs(torch, views)
     ebufs, eouts = _outputs(torch, views)
     rig.pose(torch, 0)
