@@ -89,3 +89,21 @@ def test_split_frame_ordinary_views(ctx, floor50k_scene):
     one, _ = ctx.render_host_ex(views, STREAMS)
     _same(split, one, "ordinary views")
     ctx.synchronize()
+
+
+def test_split_frame_mixed_depths(ctx, floor50k_scene):
+    """One batch with views at the full depth and below the trees' depth
+    (whose rays the box test cannot clear, so every such pixel is handed
+    on): every stream equals the one-launch frame's."""
+    import qubatron_gb300._lib as L
+    from qubatron_gb300 import view_setup
+    _character_scene(ctx, floor50k_scene)
+    pose = ((500.2, 600.9, 1500.3), (-0.4, -0.45, 0.0), 1.1)
+    views = [view_setup(320, 200, *pose, 10, ml, S, 1, 0.0) for ml in (LEVELS, LEVELS - 3, LEVELS)]
+    ctx.set_option(L.OPT_SPLIT_TREES, 1)
+    split, st = ctx.render_host_ex(views, STREAMS)
+    assert st["queued"] >= 320 * 200 // 2  # at least the shallow view's hits
+    ctx.set_option(L.OPT_SPLIT_TREES, 0)
+    one, _ = ctx.render_host_ex(views, STREAMS)
+    _same(split, one, "mixed depths")
+    ctx.synchronize()
