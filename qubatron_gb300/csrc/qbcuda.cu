@@ -907,7 +907,8 @@ int launch_simple(qbc_ctx* c, const qbc::Batch& b, size_t smem) {
 // next ray may not (with its state and the phase to resume at); the
 // two-tree kernel finishes the queued pixels, then the tiles the one-tree
 // kernel left. A pixel leaves the one-tree kernel at most once. The queue
-// holds a quarter of the batch's pixels; once it may not hold every pixel
+// holds a quarter of the batch's pixels (kSplitRecWords words each, two
+// record units of the context's buffer); once it may not hold every pixel
 // in flight (at most 64 per warp after a warp's last look at the count: the
 // 32 in its lanes and a new tile's 32), the one-tree kernel takes no new
 // tile.

@@ -169,8 +169,8 @@ enum Stat : int {
 };
 
 struct Wave {
-  uint32_t* rec;                // records (kRecWords words each)
-  unsigned int* qcount;         // records written by the primary pass
+  uint32_t* rec;                // records (kRecWords words each; kSplitRecWords in a split frame)
+  unsigned int* qcount;         // records written (by the primary pass, or a split frame's one-tree kernel)
   unsigned int* qnext;          // shade-pass work counter
   unsigned long long* stats;    // kStatCount counters
   uint32_t cap;                 // record capacity
