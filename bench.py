@@ -620,6 +620,135 @@ def proposal_sweep(ctx, qb, views, outs, stream, update, args):
             "timing": "eager two-pass frames, median of 3 after one untimed"}
 
 
+def measure_paths(ctx, scene, stream, hbm_gbs: float) -> dict:
+    """The traversal's other clients and producers on the bench's static
+    scene, each on device arrays timed with CUDA events, beside the oracle's
+    CPU version of the same work on a sample:
+    - ray queries (qbc_trace_rays; oracle: qbo_trace on all host threads),
+      8M seeded rays from inside the basecube; the oracle's status, leaf and
+      model index must equal the GPU's on its sample;
+    - the bulk build of the static tree from all points (qbc_build_tree;
+      oracle: octree_insert_point in order, one thread, on a prefix of the
+      points); the node count must equal the host producer's;
+    - static edits, octree_remove_point of 1 % of the points in order
+      (qbc_tree_remove_points; oracle: the same sequence on a copy of the
+      node array, one thread); model and parent indices must be equal.
+    The ray queries' algorithmic bytes count 32 B per node visit and 28 B
+    per leaf hit (the leaf-box words are not counted: a lower bound)."""
+    import ctypes as C
+    import torch
+    import qubatron_gb300 as qb
+    from oracle import qbo
+    spec = scene.spec
+    S, L = float(spec.basesize), int(spec.levels)
+    threads = os.cpu_count() or 1
+
+    def timed(fn, reps=3, setup=None):
+        ts = []
+        for r in range(reps + 1):
+            if setup:
+                setup()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            if r:
+                ts.append(a.elapsed_time(b))
+        return statistics.median(ts)
+
+    res = {}
+    # -- ray queries --
+    n = 8 << 20
+    gen = torch.Generator(device="cuda").manual_seed(5)
+    pos = (torch.rand((n, 3), generator=gen, device="cuda") * S).contiguous()
+    d = torch.randn((n, 3), generator=gen, device="cuda")
+    d = (d / d.norm(dim=1, keepdim=True)).contiguous()
+    status = torch.empty(n, dtype=torch.int32, device="cuda")
+    leaf = torch.empty((n, 2), dtype=torch.int32, device="cuda")
+    model = torch.empty((n, 2), dtype=torch.int32, device="cuda")
+    visits = torch.empty((n, 2), dtype=torch.int32, device="cuda")
+    hits = qb._lib.RayHits(status.data_ptr(), leaf.data_ptr(), model.data_ptr(), None, None, None,
+                           visits.data_ptr())
+    bc = (C.c_float * 4)(0.0, S, S, S)
+
+    def query():
+        qb._lib.check(ctx._lib.qbc_trace_rays(ctx.handle, C.c_void_p(pos.data_ptr()), C.c_void_p(d.data_ptr()), n,
+                                              bc, L, C.byref(hits), 1))
+
+    ms = timed(query)
+    n_vis = int(visits.to(torch.int64).sum())
+    n_leaf = int((status == 1).sum())
+    alg = 32.0 * n_vis + 28.0 * n_leaf
+    k = 1 << 18
+    sc = qbo.Scene(scene.nodes, scene.colors, scene.normals)
+    hp, hd = pos[:k].cpu().numpy(), d[:k].cpu().numpy()
+    t0 = time.perf_counter()
+    cpu = qbo.trace_rays(sc, (0.0, S, S, S), L, hp, hd, threads)
+    cpu_s = time.perf_counter() - t0
+    bad = int((cpu["status"] != status[:k].cpu().numpy()).sum()
+              + (cpu["leaf"] != leaf[:k].cpu().numpy()).any(axis=1).sum()
+              + (cpu["model"] != model[:k].cpu().numpy()).any(axis=1).sum())
+    res["ray_queries"] = {
+        "rays": n, "ms": round(ms, 3), "mrays_per_s": n / ms / 1e3, "leaf_hits": n_leaf, "node_visits": n_vis,
+        "roofline": {"bound": "hbm", "achieved": alg / (ms / 1e3) / 1e9, "peak": hbm_gbs, "unit": "GB/s",
+                     "frac": alg / (ms / 1e3) / 1e9 / hbm_gbs,
+                     "algorithmic": "32 B per node visit + 28 B per leaf hit (leaf-box words not counted)"},
+        "cpu_baseline": {"value": k / cpu_s / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": f"the first {k} rays"},
+        "parity_sample": {"rays": k, "mismatches": bad, "streams": "status, leaf, model"}}
+    del pos, d, status, leaf, model, visits
+    # -- bulk build of the static tree --
+    pts = torch.from_numpy(np.ascontiguousarray(scene.points, np.float32)).cuda()
+    npts = int(pts.shape[0])
+
+    def build():
+        ctx.build_tree(False, (pts.data_ptr(), npts), S, L, count=False)
+
+    ms = timed(build)
+    nodes = ctx.tree_nodes(0)
+    m = min(npts, 2_000_000)
+    t0 = time.perf_counter()
+    qbo.build_tree(scene.points[:m], S, L)
+    cpu_s = time.perf_counter() - t0
+    res["bulk_build"] = {
+        "points": npts, "ms": round(ms, 3), "mpoints_per_s": npts / ms / 1e3, "nodes": nodes,
+        "nodes_equal_host_producer": nodes == int(scene.nodes.shape[0]),
+        "cpu_baseline": {"value": m / cpu_s / 1e6, "unit": "Mpoints/s", "cores": 1, "kind": "port",
+                         "sample": f"the first {m} points into an empty tree"}}
+    # -- static edits: remove 1 % of the points, in a seeded order --
+    rng = np.random.default_rng(9)
+    sel = np.ascontiguousarray(scene.points[rng.choice(npts, npts // 100, replace=False)], np.float32)
+    nsel = sel.shape[0]
+    sel_d = torch.from_numpy(sel).cuda()
+    mod = torch.empty(nsel, dtype=torch.int32, device="cuda")
+    par = torch.empty(nsel, dtype=torch.int32, device="cuda")
+    removed = C.c_int64()
+    i32 = C.POINTER(C.c_int32)
+
+    def remove():
+        fp = C.cast(C.c_void_p(sel_d.data_ptr()), qb._lib.c_float_p)
+        qb._lib.check(ctx._lib.qbc_tree_remove_points(ctx.handle, 0, fp, nsel, S, L, 1,
+                                                      C.cast(C.c_void_p(mod.data_ptr()), i32),
+                                                      C.cast(C.c_void_p(par.data_ptr()), i32), C.byref(removed)))
+
+    ms = timed(remove, setup=build)  # each edit on a freshly built tree
+    host = np.ascontiguousarray(scene.nodes, np.int32).copy()
+    t0 = time.perf_counter()
+    cmod, cpar = qbo.remove_points(host, sel, S, L)
+    cpu_s = time.perf_counter() - t0
+    res["static_edits"] = {
+        "points_removed": nsel, "ms": round(ms, 3), "mpoints_per_s": nsel / ms / 1e3, "removed": removed.value,
+        "cpu_baseline": {"value": nsel / cpu_s / 1e6, "unit": "Mpoints/s", "cores": 1, "kind": "port",
+                         "sample": f"all {nsel} removals on a copy of the node array"},
+        "parity": {"model_and_parent_equal": bool(np.array_equal(cmod, mod.cpu().numpy())
+                                                  and np.array_equal(cpar, par.cpu().numpy()))}}
+    ctx.build_tree(False, (pts.data_ptr(), npts), S, L)  # leave the tree whole
+    torch.cuda.synchronize()
+    return res
+
+
 def run_gpu(args):
     import torch
     import qubatron_gb300 as qb
@@ -934,6 +1063,9 @@ def run_gpu(args):
         line["parity_sample"] = res.pop("parity")
         line["parity_sample"]["streams"] = "rgba8, flags, leaf (GPU frame vs the oracle on the CPU sample's pixels)"
         line["cpu_baseline"] = {k: v for k, v in res.items() if k not in ("seconds", "rays")}
+    if args.paths and world == 1 and scene.nodes is not None and character is None:
+        # last: it rebuilds and edits the static tree
+        line["paths"] = measure_paths(ctx, scene, stream, peaks()[0])
     ctx.close()
     if rank == 0:
         print(json.dumps(line))
@@ -954,6 +1086,8 @@ def main():
     ap.add_argument("--service-min", type=int, default=0, help="set the service threshold (no autotune)")
     ap.add_argument("--tile-width", type=int, default=0, help="set the warp tile width 4/8/16/32 (no autotune)")
     ap.add_argument("--blocks-per-sm", type=int, default=0, help="set render blocks per SM (no autotune)")
+    ap.add_argument("--paths", action="store_true",
+                    help="also time ray queries, the GPU bulk build and static edits on the scene (with the oracle)")
     ap.add_argument("--split-trees", type=int, default=-1, choices=[-1, 0, 1],
                     help="two-tree fused frames: 1 one-tree + two-tree launch, 0 one launch (-1: library default)")
     ap.add_argument("--workload", default=None)

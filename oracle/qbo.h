@@ -128,6 +128,11 @@ typedef struct qbo_frame
 /* Traversal: cube_trace_line(pos, dir) (octree_fsh.c:138-379). */
 void qbo_trace(const qbo_scene* sc, const float basecube[4], int maxlevel, const float pos[3], const float dir[3], qbo_hit* out);
 
+/* qbo_trace over n rays on `threads` host threads (0: all); per ray status,
+ * leaf[2], model[2], visits[2] (any output may be NULL). */
+void qbo_trace_rays(const qbo_scene* sc, const float basecube[4], int maxlevel, const float* pos, const float* dir,
+                    int64_t n, int32_t* status, int32_t* leaf, int32_t* model, int32_t* visits, int threads);
+
 /* One fragment: main() (octree_fsh.c:399-464) at pixel (i, j), j from the bottom. */
 void qbo_shade_pixel(const qbo_scene* sc, const qbo_view* v, int i, int j, float rgba[4], uint32_t* flags, int32_t leaf[4], float isp[4], uint32_t visits[4]);
 
@@ -173,6 +178,9 @@ uint8_t qbo_unorm8(float f);
 int  qbo_insert_point(int32_t* nodes, int64_t* len, int64_t cap, float basesize, int levels, int64_t modind, const float pnt[3], int32_t* octindarr);
 int  qbo_insert_path(int32_t* nodes, int64_t* len, int64_t cap, int levels, int64_t modind, const int32_t* octets);
 void qbo_remove_point(int32_t* nodes, float basesize, int levels, const float pnt[3], int32_t* modind, int32_t* octind);
+/* qbo_remove_point for n points (3 floats each) in order. */
+void qbo_remove_points(int32_t* nodes, float basesize, int levels, const float* pnts, int64_t n, int32_t* modind,
+                       int32_t* octind);
 void qbo_point_octets(float basesize, int levels, const float pnt[3], int32_t* octets);
 /* All n points in order into an empty tree; returns the node count or -1. */
 int64_t qbo_build_tree(const float* pnts, int64_t n, float basesize, int levels, int32_t* nodes, int64_t cap);

@@ -108,6 +108,9 @@ def qbo() -> C.CDLL:
         lib.qbo_render_pixels.argtypes = [C.POINTER(QboScene), C.POINTER(QboView), i32p, i32p, C.c_int64,
                                           C.POINTER(QboFrame), C.c_int]
         lib.qbo_render_pixels.restype = None
+        lib.qbo_trace_rays.argtypes = [C.POINTER(QboScene), C.POINTER(C.c_float), C.c_int, f32p, f32p, C.c_int64,
+                                       i32p, i32p, i32p, i32p, C.c_int]
+        lib.qbo_trace_rays.restype = None
         lib.qbo_view_setup.argtypes = [C.c_float, C.c_float, f32p, f32p, C.c_float, C.c_int, C.c_int, C.c_float,
                                        C.c_int, C.c_float, C.POINTER(QboView)]
         lib.qbo_view_setup.restype = None
@@ -119,6 +122,8 @@ def qbo() -> C.CDLL:
         lib.qbo_insert_path.restype = C.c_int
         lib.qbo_remove_point.argtypes = [i32p, C.c_float, C.c_int, f32p, i32p, i32p]
         lib.qbo_remove_point.restype = None
+        lib.qbo_remove_points.argtypes = [i32p, C.c_float, C.c_int, f32p, C.c_int64, i32p, i32p]
+        lib.qbo_remove_points.restype = None
         lib.qbo_point_octets.argtypes = [C.c_float, C.c_int, f32p, i32p]
         lib.qbo_build_boxes.argtypes = [i32p, C.c_int64, u32p]
         lib.qbo_build_boxes.restype = C.c_int32
@@ -240,6 +245,35 @@ def render(scene: Scene, view: QboView, threads: int = 0, streams=("rgba", "rgba
         setattr(fr, s, a.ctypes.data_as(shapes[s][2]))
     qbo().qbo_render(C.byref(scene.c), C.byref(view), C.byref(fr), int(threads))
     return out
+
+
+def trace_rays(scene: Scene, basecube, maxlevel: int, pos: np.ndarray, dirs: np.ndarray, threads: int = 0) -> dict:
+    """qbo_trace over a batch of rays on host threads -> status, leaf,
+    model and visits arrays."""
+    pos = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+    dirs = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+    n = pos.shape[0]
+    out = {"status": np.zeros(n, np.int32), "leaf": np.zeros((n, 2), np.int32), "model": np.zeros((n, 2), np.int32),
+           "visits": np.zeros((n, 2), np.int32)}
+    bc = (C.c_float * 4)(*[float(x) for x in basecube])
+    qbo().qbo_trace_rays(C.byref(scene.c), bc, int(maxlevel), pos.ctypes.data_as(f32p), dirs.ctypes.data_as(f32p), n,
+                         out["status"].ctypes.data_as(i32p), out["leaf"].ctypes.data_as(i32p),
+                         out["model"].ctypes.data_as(i32p), out["visits"].ctypes.data_as(i32p), int(threads))
+    return out
+
+
+def remove_points(nodes: np.ndarray, points: np.ndarray, basesize: float = 1800.0, levels: int = 12):
+    """octree_remove_point restatement for each point in order, editing
+    nodes (a C-contiguous int32 (n, 12) array) in place -> (modind, octind),
+    -1 where a walk met an empty link."""
+    assert nodes.dtype == np.int32 and nodes.flags["C_CONTIGUOUS"]
+    pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    n = pts.shape[0]
+    mod = np.full(n, -1, np.int32)
+    oct_ = np.full(n, -1, np.int32)
+    qbo().qbo_remove_points(nodes.ctypes.data_as(i32p), basesize, levels, pts.ctypes.data_as(f32p), n,
+                            mod.ctypes.data_as(i32p), oct_.ctypes.data_as(i32p))
+    return mod, oct_
 
 
 def render_pixels(scene: Scene, view: QboView, px: np.ndarray, py: np.ndarray, threads: int = 0):

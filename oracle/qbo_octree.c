@@ -103,3 +103,12 @@ void qbo_remove_point(int32_t* nodes, float basesize, int levels, const float pn
         if (index == 0) return;
     }
 }
+
+/* n qbo_remove_point calls in input order (the reference's sequence of
+ * octree_remove_point calls); a point whose walk meets an empty link leaves
+ * its modind / octind entries as they were. */
+void qbo_remove_points(int32_t* nodes, float basesize, int levels, const float* pnts, int64_t n, int32_t* modind,
+                       int32_t* octind)
+{
+    for (int64_t k = 0; k < n; k++) qbo_remove_point(nodes, basesize, levels, pnts + 3 * k, modind + k, octind + k);
+}

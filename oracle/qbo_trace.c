@@ -664,3 +664,38 @@ void qbo_render_pixels(const qbo_scene* sc, const qbo_view* v, const int32_t* px
     for (int64_t k = 0; k < n; k++) write_pixel(sc, v, px[k], py[k], k, out);
     (void) threads;
 }
+
+/* A batch of ray queries, rays k = 0..n-1 (pos, dir: 3 floats each), on
+ * `threads` host threads (0: all): per ray its status, leaf node indices,
+ * model indices and visits (any output may be NULL). The CPU side of the
+ * library's batched queries (qbc_trace_rays); each ray is qbo_trace. */
+void qbo_trace_rays(const qbo_scene* sc, const float basecube[4], int maxlevel, const float* pos, const float* dir,
+                    int64_t n, int32_t* status, int32_t* leaf, int32_t* model, int32_t* visits, int threads)
+{
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 256) num_threads(threads)
+#endif
+    for (int64_t k = 0; k < n; k++)
+    {
+        qbo_hit h;
+        qbo_trace(sc, basecube, maxlevel, pos + 3 * k, dir + 3 * k, &h);
+        if (status) status[k] = h.status;
+        if (leaf)
+        {
+            leaf[2 * k]     = h.leaf[0];
+            leaf[2 * k + 1] = h.leaf[1];
+        }
+        if (model)
+        {
+            model[2 * k]     = h.model[0];
+            model[2 * k + 1] = h.model[1];
+        }
+        if (visits)
+        {
+            visits[2 * k]     = h.visits[0];
+            visits[2 * k + 1] = h.visits[1];
+        }
+    }
+    (void) threads;
+}
