@@ -139,3 +139,37 @@ def test_unorm8(oracle):
     lib = oracle.qbo()
     for f, u in [(0.0, 0), (-1.0, 0), (float("nan"), 0), (1.0, 255), (2.0, 255), (0.5, 128), (1.0 / 255.0, 1)]:
         assert lib.qbo_unorm8(f) == u
+
+
+def test_batched_entry_points_equal_single_calls(oracle):
+    """qbo_trace_rays (threads) and qbo_remove_points (in order) equal the
+    single-ray and single-point calls they batch."""
+    from qubatron_gb300 import scenes
+    spec = scenes.scaled_spec("floor1m", 40_000)
+    pts = scenes.generate_points(spec)[0]
+    nodes = oracle.build_tree(pts, S, LEVELS)
+    col = np.ones((pts.shape[0], 3), np.float32)
+    sc = oracle.Scene(nodes, col, col)
+    rng = np.random.default_rng(5)
+    pos = rng.uniform(0, S, (1500, 3)).astype(np.float32)
+    d = rng.normal(size=(1500, 3)).astype(np.float32)
+    # a third of the rays aimed at surface points: many hits
+    pos[:500] = (903.7, 421.3, 1702.9)
+    d[:500] = pts[rng.choice(pts.shape[0], 500)] - pos[:500]
+    bc = (0.0, S, S, S)
+    out = oracle.trace_rays(sc, bc, LEVELS, pos, d, threads=4)
+    assert (out["status"] == 1).sum() > 50
+    for i in range(pos.shape[0]):
+        h = oracle.trace(sc, bc, LEVELS, pos[i], d[i])
+        assert (h.status, tuple(h.leaf[:]), tuple(h.model[:]), tuple(h.visits[:])) == (
+            out["status"][i], tuple(out["leaf"][i]), tuple(out["model"][i]), tuple(out["visits"][i])), i
+    a, b = nodes.copy(), nodes.copy()
+    sel = np.concatenate([pts[rng.choice(pts.shape[0], 300, replace=False)], pts[:20]])  # with repeats
+    m1, o1 = oracle.remove_points(a, sel, S, LEVELS)
+    lib = oracle.qbo()
+    for i in range(sel.shape[0]):
+        mi, oi = np.full(1, -1, np.int32), np.full(1, -1, np.int32)
+        lib.qbo_remove_point(b.ctypes.data_as(oracle.i32p), S, LEVELS, np.ascontiguousarray(sel[i]).ctypes.data_as(
+            oracle.f32p), mi.ctypes.data_as(oracle.i32p), oi.ctypes.data_as(oracle.i32p))
+        assert (m1[i], o1[i]) == (mi[0], oi[0]), i
+    assert np.array_equal(a, b)
