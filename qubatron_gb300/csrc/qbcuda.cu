@@ -1169,6 +1169,22 @@ int render_views_impl(qbc_ctx* c, const qbc_view* views, const qbc_outputs* outs
   return read_stats(c, stats, two);
 }
 
+// Ray queries: one wave of resident blocks (lanes take rays by grid stride),
+// never more blocks than the rays need.
+template <bool EXACT, bool DYN>
+int launch_rays(qbc_ctx* c, const qbc::RayJob& job, size_t smem) {
+  auto kern = qbc::rays_kernel<EXACT, DYN>;
+  int per_sm = 0;
+  QBC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, qbc::kThreads, smem));
+  if (per_sm < 1) return fail(QBC_E_STATE, "rays_kernel: no block fits on an SM with %zu B shared memory", smem);
+  const int64_t blocks = std::max<int64_t>(
+      1, std::min<int64_t>((int64_t)per_sm * c->sm_count, (job.n + qbc::kThreads - 1) / qbc::kThreads));
+  kern<<<(unsigned)blocks, qbc::kThreads, smem, c->stream>>>(device_scene(c), job);
+  QBC_CUDA(cudaGetLastError());
+  ++c->launches;
+  return QBC_OK;
+}
+
 extern "C" int qbc_trace_rays(qbc_ctx* c, const float* pos, const float* dir, int64_t n, const float basecube[4],
                               int maxlevel, const qbc_ray_hits* out, int on_device) {
   qbc::clear_error();
@@ -1235,21 +1251,13 @@ extern "C" int qbc_trace_rays(qbc_ctx* c, const float* pos, const float* dir, in
   job.o.col = (float*)dv[4];
   job.o.nrm = (float*)dv[5];
   job.o.visits = (uint32_t*)dv[6];
+  job.service_min = c->service_min;
   const bool dyn = c->tree[1].n > 0;
-  size_t smem = (size_t)maxlevel * (dyn ? 3 : 2) * qbc::kThreads * sizeof(uint32_t);
-  int64_t blocks = (n + qbc::kThreads - 1) / qbc::kThreads;
-  if (blocks > INT32_MAX) return fail(QBC_E_ARG, "qbc_trace_rays: too many rays");
+  const size_t smem = (size_t)maxlevel * (dyn ? 3 : 2) * qbc::kThreads * sizeof(uint32_t);
   const bool exact = qbc::cube_shift_exact(probe);
-  if (exact && dyn)
-    qbc::rays_kernel<true, true><<<(unsigned)blocks, qbc::kThreads, smem, c->stream>>>(device_scene(c), job);
-  else if (exact)
-    qbc::rays_kernel<true, false><<<(unsigned)blocks, qbc::kThreads, smem, c->stream>>>(device_scene(c), job);
-  else if (dyn)
-    qbc::rays_kernel<false, true><<<(unsigned)blocks, qbc::kThreads, smem, c->stream>>>(device_scene(c), job);
-  else
-    qbc::rays_kernel<false, false><<<(unsigned)blocks, qbc::kThreads, smem, c->stream>>>(device_scene(c), job);
-  QBC_CUDA(cudaGetLastError());
-  ++c->launches;
+  int rc = exact ? (dyn ? launch_rays<true, true>(c, job, smem) : launch_rays<true, false>(c, job, smem))
+                 : (dyn ? launch_rays<false, true>(c, job, smem) : launch_rays<false, false>(c, job, smem));
+  if (rc) return rc;
   if (!on_device) {
     for (int k = 0; k < 7; ++k)
       if (*hs[k]) QBC_CUDA(cudaMemcpyAsync(*hs[k], dv[k], (size_t)n * bytes[k], cudaMemcpyDeviceToHost, c->stream));

@@ -858,41 +858,73 @@ struct RayJob {
   int64_t n;
   float4 bc;
   int32_t maxlevel;
-  int32_t pad;
+  int32_t service_min;  // waiting lanes that start a service (1..32)
   qbc_ray_hits o;
 };
 
+// Batched ray queries (qbc_trace_rays), on the render kernel's schedule: a
+// lane walks a sequence of rays (grid stride); a lane whose ray ended waits
+// until service_min lanes of its warp wait (or none runs), then they write
+// their results and start their next rays together, and the warp votes on
+// the division by reciprocals for the rays now running.
 template <bool EXACT, bool DYN>
 __global__ void __launch_bounds__(kThreads) rays_kernel(DevScene sc, const __grid_constant__ RayJob job) {
   extern __shared__ uint32_t smem[];
-  const int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x;
-  if (i >= job.n) return;
   Stack st{smem + threadIdx.x, kThreads};
   Walker<EXACT, DYN> w;
-  float3 p = make_float3(job.pos[3 * i], job.pos[3 * i + 1], job.pos[3 * i + 2]);
-  float3 d = make_float3(job.dir[3 * i], job.dir[3 * i + 1], job.dir[3 * i + 2]);
-  int r = w.start(job.bc, p, d, sc, job.maxlevel);
-  if (r != kDiscard) {
-    do {
-      r = w.step(sc, job.maxlevel, job.bc, st, false);
-    } while (r == kRunning);
+  const int64_t stride = (int64_t)gridDim.x * kThreads;
+  int64_t i = blockIdx.x * (int64_t)kThreads + threadIdx.x;  // the lane's current ray
+  int r = kMiss;
+  bool running = false, ended = false;  // ended: ray i is done and not yet written
+  bool fast = false;                    // warp-uniform
+  for (;;) {
+    const unsigned run = __ballot_sync(0xFFFFFFFFu, running);
+    if (run == 0u || 32 - __popc(run) >= job.service_min) {
+      if (!running) {
+        for (;;) {
+          if (ended) {
+            int32_t ms = -1, md = -1, ls = -1, ld = -1;
+            float4 col = make_float4(0.f, 0.f, 0.f, 0.f), nrm = col, isp = col;
+            if (r == kLeaf) {
+              w.leaf(sc, ms, md, col, nrm);
+              isp = w.e;
+              ls = w.ns;
+              ld = w.nd;
+            }
+            const qbc_ray_hits& o = job.o;
+            if (o.status) o.status[i] = r == kDiscard ? kDiscard : (r == kLeaf ? kLeaf : kMiss);
+            if (o.leaf) reinterpret_cast<int2*>(o.leaf)[i] = make_int2(ls, ld);
+            if (o.model) reinterpret_cast<int2*>(o.model)[i] = make_int2(ms, md);
+            if (o.isp) reinterpret_cast<float4*>(o.isp)[i] = isp;
+            if (o.col) reinterpret_cast<float4*>(o.col)[i] = col;
+            if (o.nrm) reinterpret_cast<float4*>(o.nrm)[i] = nrm;
+            if (o.visits)
+              reinterpret_cast<uint2*>(o.visits)[i] = r == kDiscard ? make_uint2(0, 0) : make_uint2(w.vis_s, w.vis_d);
+            ended = false;
+            i += stride;
+          }
+          if (i >= job.n) break;
+          const float3 p = make_float3(job.pos[3 * i], job.pos[3 * i + 1], job.pos[3 * i + 2]);
+          const float3 d = make_float3(job.dir[3 * i], job.dir[3 * i + 1], job.dir[3 * i + 2]);
+          r = w.start(job.bc, p, d, sc, job.maxlevel);
+          if (r != kDiscard) {
+            running = true;
+            break;
+          }
+          ended = true;  // written on the next pass of this loop
+        }
+      }
+      if (__ballot_sync(0xFFFFFFFFu, running) == 0u) break;  // no ray left for any lane
+      fast = EXACT && __all_sync(0xFFFFFFFFu, !running || (w.mode & 1u));
+    }
+    if (running) {
+      r = w.step(sc, job.maxlevel, job.bc, st, fast);
+      if (r != kRunning) {
+        running = false;
+        ended = true;
+      }
+    }
   }
-  int32_t ms = -1, md = -1, ls = -1, ld = -1;
-  float4 col = make_float4(0.f, 0.f, 0.f, 0.f), nrm = col, isp = col;
-  if (r == kLeaf) {
-    w.leaf(sc, ms, md, col, nrm);
-    isp = w.e;
-    ls = w.ns;
-    ld = w.nd;
-  }
-  const qbc_ray_hits& o = job.o;
-  if (o.status) o.status[i] = r == kDiscard ? kDiscard : (r == kLeaf ? kLeaf : kMiss);
-  if (o.leaf) reinterpret_cast<int2*>(o.leaf)[i] = make_int2(ls, ld);
-  if (o.model) reinterpret_cast<int2*>(o.model)[i] = make_int2(ms, md);
-  if (o.isp) reinterpret_cast<float4*>(o.isp)[i] = isp;
-  if (o.col) reinterpret_cast<float4*>(o.col)[i] = col;
-  if (o.nrm) reinterpret_cast<float4*>(o.nrm)[i] = nrm;
-  if (o.visits) reinterpret_cast<uint2*>(o.visits)[i] = r == kDiscard ? make_uint2(0, 0) : make_uint2(w.vis_s, w.vis_d);
 }
 
 }  // namespace qbc
